@@ -1,0 +1,95 @@
+"""Seeded synthetic particle sets for the SPH hot path.
+
+These stand in for the reference's setup generators and benchmark inputs (no
+dataset is involved): every generator is deterministic given its seed.
+
+- ``sedov_taylor``: FCC lattice of 4*n^3 equal-mass particles in the periodic
+  unit cube, rho = 1, u = 1e-5, total energy E added uniformly to the internal
+  energy of the particles within r < r_inj * a of the centre (a = 1/n), optional
+  Gaussian position jitter sigma * a.
+- ``clustered_box``: half the particles uniform in the unit cube, half in a
+  Gaussian clump (clipped into the box), v ~ N(0, 0.1^2), u ~ U[0.5, 1.5].
+- ``sound_wave``: FCC lattice trimmed to 2^18 particles with a 1e-4 sin(2 pi x)
+  density perturbation applied by a position remap.
+
+h is initialised to hfact * (m / rho)^(1/3) with the local density estimate of
+the generator (hfact = 1.2 for M4).
+"""
+
+import numpy as np
+
+HFACT_M4 = 1.2
+
+
+def fcc_lattice(n, box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0)):
+    """4*n^3 positions of a cubic FCC lattice filling the box, in i-j-k-basis order.
+
+    Lattice sites sit at ((i, j, k) + basis + 1/4) * a so that no particle lies on a
+    box face."""
+    bmin = np.asarray(box_min, float)
+    a = (np.asarray(box_max, float) - bmin) / n
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]]) + 0.25
+    idx = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1)
+    idx = idx.reshape(-1, 1, 3).astype(float)
+    pos = (idx + basis[None, :, :]).reshape(-1, 3) * a + bmin
+    return pos
+
+
+def sedov_taylor(n_cells, jitter=0.0, seed=1, E=1.0, u0=1e-5, r_inj=2.0, gamma=5.0 / 3.0):
+    pos = fcc_lattice(n_cells)
+    N = pos.shape[0]
+    a = 1.0 / n_cells
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        pos = pos + rng.normal(0.0, jitter * a, size=pos.shape)
+        pos = np.mod(pos, 1.0)
+    pmass = 1.0 / N
+    u = np.full(N, u0)
+    r = np.linalg.norm(pos - 0.5, axis=1)
+    inj = r < r_inj * a
+    n_inj = int(inj.sum())
+    if n_inj:
+        u[inj] += E / (pmass * n_inj)
+    h = np.full(N, HFACT_M4 * (pmass / 1.0) ** (1.0 / 3.0))
+    return dict(pos=pos, vel=np.zeros((N, 3)), h=h, u=u, pmass=pmass, gamma=gamma,
+                box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0), periodic=True,
+                n_inject=n_inj)
+
+
+def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0):
+    rng = np.random.default_rng(seed)
+    n1 = N // 2
+    n2 = N - n1
+    p1 = rng.random((n1, 3))
+    p2 = np.clip(rng.normal(0.5, sigma, size=(n2, 3)), 1e-9, 1.0 - 1e-9)
+    pos = np.concatenate([p1, p2])
+    vel = rng.normal(0.0, 0.1, size=(N, 3))
+    u = rng.uniform(0.5, 1.5, size=N)
+    pmass = 1.0 / N
+    # local density estimate of the two populations
+    rho_uniform = 0.5
+    r = pos - 0.5
+    rho_clump = 0.5 * np.exp(-0.5 * np.sum(r * r, 1) / sigma**2) / ((2 * np.pi) ** 1.5 * sigma**3)
+    rho = np.maximum(rho_uniform + rho_clump, 1e-3)
+    h = HFACT_M4 * (pmass / rho) ** (1.0 / 3.0)
+    return dict(pos=pos, vel=vel, h=h, u=u, pmass=pmass, gamma=gamma,
+                box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0), periodic=True)
+
+
+def sound_wave(n_target=1 << 18, n_cells=41, amp=1e-4, gamma=1.0001, cs=1.0, seed=12345):
+    """FCC 4*41^3 lattice trimmed to the first n_target sites in lattice order, then a
+    density perturbation rho = 1 + amp sin(2 pi x) by the x -> x - amp/(2 pi) cos(2 pi x)
+    remap (first order).  Trimming leaves a partial final plane, which is fine for a
+    differentiable-step test case."""
+    pos = fcc_lattice(n_cells)[:n_target]
+    N = pos.shape[0]
+    x = pos[:, 0]
+    pos = pos.copy()
+    pos[:, 0] = np.mod(x - amp / (2 * np.pi) * np.cos(2 * np.pi * x), 1.0)
+    pmass = 1.0 / N
+    rho = 1.0 + amp * np.sin(2 * np.pi * pos[:, 0])
+    P0 = cs * cs / gamma
+    u = np.full(N, P0 / ((gamma - 1.0) * 1.0))
+    h = HFACT_M4 * (pmass / rho) ** (1.0 / 3.0)
+    return dict(pos=pos, vel=np.zeros((N, 3)), h=h, u=u, pmass=pmass, gamma=gamma,
+                box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0), periodic=True)
