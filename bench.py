@@ -1,0 +1,448 @@
+"""Benchmark of the GB300 SPH timestep hot path (one JSON line on stdout, rank 0).
+
+Workload (SPH particle-steps/s): Sedov-Taylor blast, FCC lattice 4*64^3 = 1,048,576
+equal-mass particles in the periodic unit cube, Gaussian position jitter 0.05 of the
+lattice spacing (seed 1), rho = 1, u = 1e-5, E = 1 injected within r < 2 spacings,
+gamma = 5/3, M4, hfact 1.2, constant AV alpha = 1 beta = 2, CFL 0.3, tree and
+neighbour cache rebuilt every step; FP32-mixed pair arithmetic (--precision fp64
+for the FP64 path).  One step = one full Solver::evolve_once.
+
+Arms
+  default          the GB300 path: `value` is device-timed (CUDA events, inputs resident
+                   in HBM); `e2e` is the same metric through the public model API with the
+                   particle state copied from pinned host memory before and back after
+                   every step; `cpu_baseline` times the FP64 oracle on the host cores on
+                   a bounded sample; `roofline` reports the dominant stage.
+  --impl reference the reference's CPU implementation of the path: the reference cannot
+                   be built here (SYCL), so this is the FP64 oracle restatement, OpenMP on
+                   every host core, on the same workload.
+Under torchrun each rank runs an independent replica (the path does not shard across
+GPUs in this build); value = all ranks' particle-steps / max rank time.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SPH particle-steps/s (FP32-mixed vs FP64 at <=1e-5 rel err)"
+UNIT = "particle-steps/s"
+L2_BYTES = 126 * 2**20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--cells", type=int, default=64, help="FCC cells per axis (4*cells^3 particles)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=20.0,
+                   help="bounded CPU-baseline sample, seconds of host work")
+    return p.parse_args()
+
+
+def workload(cells):
+    from shamrock_gb300 import setups
+
+    s = setups.sedov_taylor(cells, jitter=0.05, seed=1)
+    name = (f"sedov_taylor_fcc_4x{cells}^3_jitter0.05_periodic (N={len(s['h'])}, M4, "
+            "constant AV a=1 b=2, gamma=5/3, CFL 0.3, tree rebuilt every step)")
+    return s, name
+
+
+def make_model(s, precision, device=0):
+    import shamrock_gb300 as sg
+
+    ctx = sg.Context(device)
+    m = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
+    cfg = m.gen_default_config()
+    cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0)
+    cfg.set_boundary_periodic()
+    cfg.set_eos_adiabatic(s["gamma"])
+    cfg.set_particle_mass(s["pmass"])
+    cfg.set_precision(precision)
+    m.set_solver_config(cfg)
+    m.resize_simulation_box(s["box_min"], s["box_max"])
+    m.set_particles(s["pos"], s["vel"], s["h"], s["u"])
+    m.set_cfl_cour(0.3)
+    m.set_cfl_force(0.3)
+    return m
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- roofline
+# Compulsory DRAM bytes per unit of each stage (neighbour-field gathers are counted as
+# L1/L2 hits; index streams and per-particle fields are counted).  units: rows (local
+# particles), entries (CSR entries), keys (sorted slots).
+def stage_bytes(stage, n, N, entries, P, precision, h_iters):
+    vec = 80 if precision == "mixed" else 88
+    table = {
+        # row_rank, row_local, cnt, off, own fields, CSR entries, caller a/du/v/u in+out, h
+        "derivs": n * (16 + vec + 128 + 8) + 4 * entries,
+        # per Newton iteration: CSR entries + own position + per-row h/eps state
+        "h_iterate": (n * (16 + (32 if precision == "mixed" else 24) + 40) + 4 * entries) * h_iters,
+        "cache_fill": n * (4 + 4 + 4 + 32) + 4 * entries,
+        "cache_count": n * (4 + 4 + 4 + 32),
+        "omega": n * (16 + 32 + 8 + 8) + 4 * entries,
+        "morton_sort": 16 * P,
+        "gather_eos": N * (4 + 4 + 8 * 8) + N * (80 if precision == "mixed" else 64),
+    }
+    return table.get(stage)
+
+
+def roofline(prof, log, n, precision, peaks_path):
+    ms = {k: v[0] for k, v in prof.items()}
+    dom = max(ms, key=ms.get)
+    launches = prof[dom][1]
+    entries = int(log["cache_size"])
+    N = n + int(log["n_ghost"])
+    P = 1 << (N - 1).bit_length()
+    h_iters = max(1, int(log["h_iterations"]))
+    nbytes = stage_bytes(dom, n, N, entries, P, precision, h_iters)
+    peak, peak_src = 6800.0, "fallback"
+    try:
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+            peak_src = "measured"
+    except (OSError, KeyError, ValueError):
+        pass
+    out = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peak, "peak_source": peak_src,
+           "launches": launches, "ms_per_launch": ms[dom] / max(launches, 1),
+           "share_of_step": ms[dom] / max(sum(ms.values()), 1e-12)}
+    if nbytes is not None and launches:
+        achieved = nbytes / (ms[dom] / launches * 1e-3) / 1e9
+        out.update(achieved=achieved, frac=achieved / peak, algorithmic_bytes=nbytes)
+    else:
+        out.update(achieved=None, frac=None, algorithmic_bytes=None)
+    out["traffic"] = traffic_from_profiles(dom, N)
+    out["stages_ms"] = {k: round(v, 4) for k, v in ms.items()}
+    return out
+
+
+def traffic_from_profiles(stage, N):
+    """DRAM bytes per launch of `stage` from the committed ncu summary, scaled to N."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == stage and not line.startswith("#"):
+                per_particle = float(parts[1])
+                return per_particle * N
+    except OSError:
+        pass
+    return None
+
+
+# ----------------------------------------------------------------------------- arms
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+        pg = dist
+    return world, rank, local, pg
+
+
+def cpu_baseline(s, seconds, threads=None):
+    """FP64 oracle (OpenMP) on the same workload, bounded to about `seconds`."""
+    from oracle import oracle as O
+
+    if threads:
+        O.set_threads(threads)
+    cores = O.get_threads()
+    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0,
+                     cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
+                     htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
+                     h_max_subcycles=100, tree_reduction_level=3, periodic=1)
+    oc.bmin[:] = list(s["box_min"])
+    oc.bmax[:] = list(s["box_max"])
+    sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
+    sim.evolve_once()  # dt = 0 step (h convergence, first CFL), untimed
+    n = len(s["h"])
+    t0 = time.time()
+    steps = 0
+    while True:
+        sim.evolve_once()
+        steps += 1
+        if time.time() - t0 >= seconds:
+            break
+    el = time.time() - t0
+    return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} FP64 oracle steps of the full workload ({n} particles) after one "
+                      f"untimed dt=0 step, {el:.1f} s, OpenMP {cores} threads"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and rank != 0:
+        return 0
+    s, name = workload(args.cells)
+    from oracle import oracle as O
+
+    O.set_threads(os.cpu_count())
+    cores = O.get_threads()
+    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0,
+                     cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
+                     htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
+                     h_max_subcycles=100, tree_reduction_level=3, periodic=1)
+    oc.bmin[:] = list(s["box_min"])
+    oc.bmax[:] = list(s["box_max"])
+    sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
+    n = len(s["h"])
+    for _ in range(max(1, min(args.warmup, 2))):
+        sim.evolve_once()
+    budget = 150.0
+    t0 = time.time()
+    steps = 0
+    while steps < args.steps:
+        sim.evolve_once()
+        steps += 1
+        if time.time() - t0 > budget:
+            break
+    el = time.time() - t0
+    value = n * steps / el
+    sample = (f"{steps} of {args.steps} requested FP64 steps of the full workload ({n} particles; "
+              f"stopped at a {budget:.0f} s budget if reached), after "
+              f"{max(1, min(args.warmup, 2))} untimed warm-up steps")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": name, "precision": "fp64", "particles": n,
+                       "implementation": "FP64 CPU restatement of the reference path (oracle/, "
+                                         "OpenMP); the reference itself needs a SYCL compiler"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def accuracy(s, m_mixed_state=None):
+    """Max / RMS relative error of rho, |a|, du/dt and v_sig-driven dt of one mixed step
+    against one FP64 step from the same initial state (the first, dt = 0, step)."""
+    import numpy as np
+
+    res = {}
+    d = {}
+    for prec in ("fp64", "mixed"):
+        m = make_model(s, prec)
+        m.evolve_once()
+        d[prec] = m.collect_data()
+    a, b = d["mixed"], d["fp64"]
+    rho_a = s["pmass"] * (1.2 / a["hpart"]) ** 3
+    rho_b = s["pmass"] * (1.2 / b["hpart"]) ** 3
+    rel = np.abs(rho_a - rho_b) / rho_b
+    res["rho"] = {"max": float(rel.max()), "rms": float(np.sqrt(np.mean(rel**2)))}
+    for k, key in (("axyz", "a"), ("duint", "du_dt"), ("omega", "omega")):
+        x, y = a[k], b[k]
+        if x.ndim > 1:
+            dx, ny = np.linalg.norm(x - y, axis=1), np.linalg.norm(y, axis=1)
+        else:
+            dx, ny = np.abs(x - y), np.abs(y)
+        res[key] = {"max": float(dx.max() / ny.max()),
+                    "rms": float(np.sqrt(np.mean(dx**2)) / np.sqrt(np.mean(ny**2)))}
+    res["definition"] = ("one step from the same state, mixed vs FP64 GPU path (the FP64 path is "
+                         "bit-identical to the FP64 oracle); rho per particle relative; a, du/dt, "
+                         "omega normalised by the field's max magnitude (max) or rms (rms)")
+    return res
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    s, name = workload(args.cells)
+    n = len(s["h"])
+    m = make_model(s, args.precision, device=local)
+    lib = m._lib()
+    for _ in range(max(args.warmup, 3)):
+        m.evolve_once()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    lib.profile(True)
+    l0 = lib.lib.gbsph_kernel_launches()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    logs = []
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            logs.append(m.evolve_once(stream=None))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = lib.lib.gbsph_kernel_launches() - l0
+    prof = lib.profile_read()
+    lib.profile(False)
+    t_ms = e0.elapsed_time(e1)
+    t_max = t_ms
+    total_particles = n * world
+    if dist:
+        t = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = total_particles * args.steps / (t_max * 1e-3)
+    clk = clocks.summary()
+
+    # end-to-end through the public API with host buffers, every step:
+    # pinned host -> device state copy, evolve_once, device -> pinned host state copy
+    e2e = None
+    if not args.no_e2e:
+        d = m._to_device()
+        names = ("xyz", "vxyz", "axyz", "hpart", "uint", "duint")
+        host = {k: torch.empty(d[k].shape, dtype=torch.float64, pin_memory=True) for k in names}
+        for k in names:
+            host[k].copy_(d[k])
+        h2d = sum(host[k].numel() * 8 for k in names)
+        steps_e2e = max(3, args.steps // 2)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(steps_e2e):
+            for k in names:
+                d[k].copy_(host[k], non_blocking=True)
+            m.evolve_once()
+            for k in names:
+                host[k].copy_(d[k], non_blocking=True)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        te = f0.elapsed_time(f1)
+        if dist:
+            t = torch.tensor([te], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": total_particles * steps_e2e / (te * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "steps": steps_e2e}
+
+    if rank != 0:
+        return 0
+    log = logs[-1]
+    rl = roofline(prof, log, n, args.precision, os.path.join(ROOT, "MEASURED_PEAKS.json"))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32-mixed" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": name, "precision": args.precision, "particles": n,
+                   "ghosts": int(log["n_ghost"]), "leaves": int(log["leaf_count"]),
+                   "cache_entries": int(log["cache_size"]),
+                   "l2": "inputs larger than L2 (fields + neighbour cache ~%d MB per step)"
+                         % ((int(log["cache_size"]) * 4 + n * 200) // 2**20),
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "e2e": e2e,
+        "roofline": rl,
+        "step_log": {k: log[k] for k in ("h_subcycles", "h_iterations", "corrector_iters",
+                                          "next_dt", "cfl_mult")},
+    }
+    if world == 1 and not args.no_accuracy:
+        line["accuracy_mixed_vs_fp64"] = accuracy(s)
+        # FP64 GPU rate on the same workload (the x3 denominator), a few steps
+        m64 = make_model(s, "fp64")
+        for _ in range(2):
+            m64.evolve_once()
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k64 = 3
+        g0.record(stream)
+        for _ in range(k64):
+            m64.evolve_once()
+        g1.record(stream)
+        torch.cuda.synchronize()
+        v64 = n * k64 / (g0.elapsed_time(g1) * 1e-3)
+        line["fp64_gpu"] = {"value": v64, "unit": UNIT, "steps": k64}
+        if args.precision == "mixed":
+            line["mixed_over_fp64"] = value / v64
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(s, args.cpu_seconds, threads=os.cpu_count())
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,237 @@
+/*
+ * gbsph.h — C ABI of the GB300-native SPH timestep hot path.
+ *
+ * A drop-in for the single-GPU path of Shamrock's shammodels::sph solver:
+ * Morton keys -> bitonic sort -> leaf reduction -> Karras tree / LBVH, the
+ * two-stage neighbour cache, the h-rho Newton iteration, Omega, the adiabatic
+ * EOS, constant-AV derivatives, v_sig / CFL and the leapfrog KDK step.
+ *
+ * Conventions
+ *  - Every entry point returns GBSPH_OK (0) or a GBSPH_ERR_* code; the message
+ *    of the last failure is gbsph_last_error(ctx).  No exception crosses the ABI.
+ *  - Array arguments are DEVICE pointers unless the parameter name ends in _host.
+ *    Scalars and small fixed arrays (box corners) are host values.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Positions/velocities/accelerations of the caller are three component
+ *    pointers sharing an element stride in doubles (gbsph_vec3): stride 1 for
+ *    structure-of-arrays, 4 for the reference's padded f64_3 with x = base,
+ *    y = base + 1, z = base + 2.
+ *  - Index spaces: "local" = the caller's particles [0, n_local); "merged" =
+ *    locals followed by periodic ghosts, as the reference's merged_xyzh.
+ *  - A context owns its scratch arena (tree, caches, ghost tables) and is used by
+ *    one host thread and one stream at a time.
+ *
+ * Citations are paths inside the Shamrock source tree.
+ */
+#ifndef GBSPH_H
+#define GBSPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBSPH_OK 0
+#define GBSPH_ERR_ARG 1           /* bad argument (maps to std::invalid_argument) */
+#define GBSPH_ERR_CUDA 2          /* CUDA runtime error */
+#define GBSPH_ERR_CAPACITY 3      /* caller buffer too small / 32-bit CSR overflow */
+#define GBSPH_ERR_NOT_CONVERGED 4 /* h iteration or corrector did not converge */
+#define GBSPH_ERR_STATE 5         /* call order violated (e.g. cache before tree) */
+
+#define GBSPH_FP64 0  /* every pair sum in FP64, bit-identical to the FP64 oracle */
+#define GBSPH_MIXED 1 /* FP32 pair arithmetic, FP64 positions/drift/h test/totals */
+
+typedef struct gbsph_ctx gbsph_ctx;
+
+typedef struct {
+    double *x, *y, *z;
+    uint32_t stride; /* element stride in doubles */
+    uint32_t pad;
+} gbsph_vec3;
+
+/* The caller-owned particle fields of one patch (PatchDataLayer fields
+ * xyz, vxyz, axyz, hpart, uint, duint of the reference's SPH layout). */
+typedef struct {
+    uint32_t n;
+    uint32_t pad;
+    gbsph_vec3 xyz, vxyz, axyz;
+    double *hpart, *uint, *duint;
+    double *omega; /* optional output, may be NULL */
+} gbsph_particles;
+
+/* Solver configuration (the hot-path subset of shammodels::sph::SolverConfig,
+ * shammodels/sph/include/shammodels/sph/SolverConfig.hpp). */
+typedef struct {
+    double gamma;                   /* adiabatic EOS */
+    double pmass;                   /* gpart_mass */
+    double alpha_u, alpha_AV, beta_AV; /* constant AV (config/AVConfig.hpp:52-54) */
+    double cfl_cour, cfl_force, cfl_mult_stiffness;
+    double htol_up_coarse, htol_up_fine; /* 1.1, 1.1 */
+    double epsilon_h;               /* 1e-6 */
+    uint32_t h_iter_per_subcycles;  /* 50 */
+    uint32_t h_max_subcycles;       /* 100 */
+    uint32_t tree_reduction_level;  /* 3 */
+    uint32_t periodic;              /* 1 periodic box, 0 free boundaries */
+    double box_min[3], box_max[3];
+    uint32_t precision;             /* GBSPH_FP64 or GBSPH_MIXED */
+    uint32_t pad;
+} gbsph_config;
+
+/* Synchronised solver state (the scheduler edges "time", "dt", "cfl_multiplier",
+ * shammodels/sph/include/shammodels/sph/Solver.hpp:99-145). */
+typedef struct {
+    double t, dt, cfl_mult;
+} gbsph_time_state;
+
+typedef struct {
+    double t, dt, next_dt, cfl_mult;
+    uint32_t n_local, n_ghost, leaf_count, h_subcycles, h_iterations, corrector_iters;
+    uint64_t cache_size;
+    double eps_v, max_eps_h;
+    double elapsed_s; /* wall time of the step (host clock, after the final sync) */
+    double rate;      /* n_local / elapsed_s, as Solver.cpp:3200 */
+} gbsph_step_log;
+
+/* ------------------------------------------------------------------ lifetime */
+int gbsph_create(gbsph_ctx **out, int device);
+void gbsph_destroy(gbsph_ctx *ctx);
+const char *gbsph_last_error(const gbsph_ctx *ctx);
+const char *gbsph_version(void);
+
+/* ------------------------------------------------------------------ tree (shamtree) */
+
+/* Morton codes of n positions (SoA) clamped to [bmin, bmax], padded to
+ * morton_count with the all-ones code.  key_bits 32 (the SPH path) or 64.
+ * Replaces shamtree::morton_code_set_from_positions, shamtree/src/MortonCodeSet.cpp:63-118. */
+int gbsph_morton_codes(gbsph_ctx *ctx, const double *x, const double *y, const double *z,
+                       uint32_t n, uint32_t morton_count, const double bmin_host[3],
+                       const double bmax_host[3], int key_bits, void *keys_out, void *stream);
+
+/* In-place key/value bitonic sort, len a power of two; identical network (and so
+ * identical order of equal keys) to shamalgs::algorithm::sort_by_key,
+ * shamalgs/src/primitives/sort_by_keys.cpp:36-43 ->
+ * shamalgs/src/details/algorithm/bitonicSort_updated_usm.cpp:285-396. */
+int gbsph_sort_by_key(gbsph_ctx *ctx, void *keys, uint32_t *vals, uint32_t len, int key_bits,
+                      void *stream);
+
+/* Full compressed-leaf BVH over n positions (SoA): Morton set over morton_count
+ * slots (0 = next power of two), sort, reduction (level), Karras topology, node
+ * AABBs and, when h != NULL, the interaction radius field max(h) * htol.
+ * Replaces CompressedLeafBVH::rebuild_from_positions, shamtree/src/CompressedLeafBVH.cpp:79-95,
+ * plus Solver::compute_presteps_rint, shammodels/sph/src/Solver.cpp:1322-1356. */
+int gbsph_build_tree(gbsph_ctx *ctx, const double *x, const double *y, const double *z,
+                     const double *h, uint32_t n, const double bmin_host[3],
+                     const double bmax_host[3], uint32_t reduction_level, double htol,
+                     int key_bits, uint32_t morton_count, void *stream);
+
+int gbsph_tree_counts(gbsph_ctx *ctx, uint32_t *morton_count_host, uint32_t *leaf_count_host);
+
+/* Copy the last tree out (each pointer may be NULL).  Node arrays follow the
+ * reference numbering: internal cells [0, L-1), leaves at offset L-1.  aabb_* are
+ * (2L-1) x 3 doubles, keys are u32 or u64 per the build's key_bits. */
+int gbsph_tree_export(gbsph_ctx *ctx, void *sorted_keys, uint32_t *sort_index, uint32_t *reduc,
+                      void *reduced_keys, uint32_t *lchild, uint32_t *rchild, uint8_t *lflag,
+                      uint8_t *rflag, uint32_t *endrange, double *aabb_min, double *aabb_max,
+                      double *rint, void *stream);
+
+/* Object query over the last tree, in DFS order (CLBVHObjectIterator::rtree_for,
+ * shamtree/include/shamtree/CLBVHObjectIterator.hpp:127-169).  mode 0: every
+ * object; mode 1: objects inside [q - s, q + s], visiting nodes whose AABB
+ * intersects that box.  Writes per-query counts; when out != NULL and capacity is
+ * large enough also the object ids.  *total_host receives the entry count. */
+int gbsph_tree_query(gbsph_ctx *ctx, const double *qx, const double *qy, const double *qz,
+                     uint32_t nq, int mode, double s, uint32_t *counts, uint32_t *out,
+                     uint64_t capacity, uint64_t *total_host, void *stream);
+
+/* ------------------------------------------------------------------ neighbour cache */
+
+/* Two-stage neighbour cache of the first n_local particles against the n_merged
+ * positions of the last gbsph_build_tree call (built with h).  Pair test
+ * !(r^2 > (h_a htol)^2 R^2 && r^2 > (h_b htol)^2 R^2), R = 2.
+ * Replaces NeighbourCache::start_neighbors_cache_2stages,
+ * shammodels/sph/src/modules/NeighbourCache.cpp:223-596. */
+int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, void *stream);
+
+int gbsph_cache_size(gbsph_ctx *ctx, uint64_t *total_host, uint64_t *leaf_total_host);
+
+/* The cache in the reference's ObjectCache layout (TreeTraversal.hpp:375-485):
+ * per local id a count and exclusive offset, entries are merged ids. */
+int gbsph_cache_export(gbsph_ctx *ctx, uint32_t *cnt, uint32_t *scanned, uint32_t *entries,
+                       void *stream);
+
+/* ------------------------------------------------------------------ SPH modules
+ * CSR arguments (cnt, scanned, entries) are in the reference ObjectCache layout.
+ * Positions and fields are merged-id SoA arrays; outputs are per local id. */
+
+/* `iters` Newton iterations of IterateSmoothingLengthDensity
+ * (shammodels/sph/src/modules/IterateSmoothingLengthDensity.cpp:28-120); iters = 1
+ * is exactly one module evaluation.  max/min eps and the largest iteration count
+ * any particle used are returned through the *_host pointers (may be NULL). */
+int gbsph_h_iterate(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
+                    const uint32_t *entries, const double *x, const double *y, const double *z,
+                    const double *h_old, double *h_new, double *eps, uint32_t n_local,
+                    double pmass, double h_evol_max, double h_evol_iter_max, uint32_t iters,
+                    double *max_eps_host, double *min_eps_host, uint32_t *iters_used_host,
+                    void *stream);
+
+/* NodeComputeOmega, shammodels/sph/src/modules/ComputeOmega.cpp:25-74. */
+int gbsph_omega(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
+                const uint32_t *entries, const double *x, const double *y, const double *z,
+                const double *h, uint32_t n_local, double pmass, double *omega, void *stream);
+
+/* ComputeEOSAdiabatic from h, shammodels/sph/src/modules/ComputeEos.cpp:153-245. */
+int gbsph_eos_adiabatic(gbsph_ctx *ctx, const double *h, const double *u, uint32_t n, double pmass,
+                        double gamma, double *P, double *cs, void *stream);
+
+/* UpdateDerivs::update_derivs_constantAV, shammodels/sph/src/modules/UpdateDerivs.cpp:88-288;
+ * with vsig != NULL also the v_sig maximum of Solver.cpp:2716-2788.
+ * precision GBSPH_FP64 or GBSPH_MIXED. */
+int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
+                         const uint32_t *entries, const double *x, const double *y,
+                         const double *z, const double *vx, const double *vy, const double *vz,
+                         const double *h, const double *omega, const double *u, const double *P,
+                         const double *cs, uint32_t n_local, uint32_t n_merged, double pmass,
+                         double alpha_u, double alpha_AV, double beta_AV, uint32_t precision,
+                         double *ax, double *ay, double *az, double *du, double *vsig,
+                         void *stream);
+
+/* Periodic ghost layer of one patch covering [bmin, bmax]
+ * (BasicSPHGhostHandler::find_interfaces + gen_id_table_interfaces +
+ * build_comm_merge_positions, shammodels/sph/src/BasicSPHGhosts.cpp:260-360,512-530).
+ * Returns the ghost count; gbsph_ghost_export then gives, per ghost, the source
+ * local id, the offset index (0..25, x-outer/z-inner order without the zero
+ * offset) and the merged positions/h (n_local + n_ghost entries). */
+int gbsph_periodic_ghosts(gbsph_ctx *ctx, gbsph_vec3 xyz, const double *h, uint32_t n_local,
+                          const double bmin_host[3], const double bmax_host[3], double htol,
+                          uint32_t *n_ghost_host, void *stream);
+int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double *mx, double *my,
+                       double *mz, double *mh, void *stream);
+
+/* ------------------------------------------------------------------ full step */
+
+/* One Solver::evolve_once on one patch (shammodels/sph/src/Solver.cpp:1942-3272):
+ * leapfrog predictor + periodic wrap, sph_prestep (ghosts, tree, neighbour cache,
+ * h iteration with restarts, Omega), corrector loop (ghost fields, EOS,
+ * derivatives, corrector, eps_v rerun test), v_sig/CFL, time/dt/multiplier update.
+ * Particle fields are updated in place; ts is read and updated. */
+int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
+                      gbsph_time_state *ts, gbsph_step_log *log, void *stream);
+
+/* ------------------------------------------------------------------ instrumentation
+ * Per-stage device time measured with CUDA events on the launching stream (the role
+ * of the reference's per-step timers, SolverStorage.hpp:111-118).  Enabling resets the
+ * totals; reading folds the recorded events in (it synchronises the context stream). */
+uint32_t gbsph_profile_kinds(void);
+/* Number of kernels this library has launched in the process so far. */
+uint64_t gbsph_kernel_launches(void);
+const char *gbsph_profile_name(uint32_t kind);
+int gbsph_profile_enable(gbsph_ctx *ctx, int on);
+int gbsph_profile_read(gbsph_ctx *ctx, double *ms_host, uint64_t *launches_host,
+                       uint64_t *units_host, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSPH_H */

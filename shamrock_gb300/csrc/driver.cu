@@ -1,0 +1,625 @@
+// C ABI of the GB300 SPH hot path (include/gbsph.h) and the one-patch
+// Solver::evolve_once orchestration (shammodels/sph/src/Solver.cpp:1942-3272).
+
+#include "../../include/gbsph.h"
+#include "gbsph_ctx.cuh"
+#include "sph_kernels.cuh"
+#include "sph_mixed.cuh"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+
+struct gbsph_ctx {
+    gbsph::Ctx c;
+};
+
+namespace gbsph {
+
+template<class K>
+cudaError_t sort_keys_dev(K *keys, u32 *vals, u32 len, cudaStream_t s);
+cudaError_t morton_codes_dev(Ctx &c, const f64 *x, const f64 *y, const f64 *z, u32 n, u32 P,
+                             int key_bits, void *out);
+cudaError_t export_boxes(Ctx &c, f64 *mn, f64 *mx, f64 *rint);
+
+unsigned long long g_kernel_launches = 0;
+
+int prof_begin(Ctx &c, int kind, u64 units) {
+    size_t need = 2 * (c.prof.used + 1);
+    while (c.prof.pool.size() < need) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return -1;
+        c.prof.pool.push_back(e);
+    }
+    int idx = (int) c.prof.used++;
+    if (c.prof.kinds.size() < c.prof.used) c.prof.kinds.resize(c.prof.used);
+    c.prof.kinds[idx] = kind;
+    c.prof.units[kind] += units;
+    c.prof.launches[kind] += 1;
+    cudaEventRecord(c.prof.pool[2 * idx], c.stream);
+    return idx;
+}
+
+void prof_end(Ctx &c, int idx) { cudaEventRecord(c.prof.pool[2 * idx + 1], c.stream); }
+
+void prof_collect(Ctx &c) {
+    for (size_t i = 0; i < c.prof.used; i++) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, c.prof.pool[2 * i], c.prof.pool[2 * i + 1]) == cudaSuccess)
+            c.prof.ms[c.prof.kinds[i]] += ms;
+    }
+    c.prof.used = 0;
+}
+
+Ctx::~Ctx() {
+    for (cudaEvent_t e : prof.pool) cudaEventDestroy(e);
+    DevBuf *bufs[] = {&scan_scratch, &d_scalars, &d_bbox, &keys, &sort_index, &flags_a, &flags_b,
+                      &offsets, &reduc, &reduced, &lchild, &rchild, &lflag, &rflag, &endrange,
+                      &parent, &boxes, &visit, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
+                      &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
+                      &owner, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
+                      &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
+                      &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2,
+                      &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
+                      &dt_part};
+    cudaSetDevice(device);
+    for (DevBuf *b : bufs) b->release(stream);
+    cudaStreamSynchronize(stream);
+    if (h_scalars) cudaFreeHost(h_scalars);
+}
+
+namespace {
+
+__global__ void k_cache_export_counts(u32 n, const u32 *__restrict__ row_local,
+                                      const u32 *__restrict__ cnt, u32 *__restrict__ out_cnt) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out_cnt[row_local[t]] = cnt[t];
+}
+__global__ void k_cache_export_entries(u32 n, const u32 *__restrict__ row_local,
+                                       const u32 *__restrict__ cnt, const u32 *__restrict__ off,
+                                       const u32 *__restrict__ ent,
+                                       const u32 *__restrict__ sort_index,
+                                       const u32 *__restrict__ out_scanned,
+                                       u32 *__restrict__ out_ent) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    u32 w = out_scanned[row_local[t]];
+    for (u32 k = off[t]; k < off[t] + cnt[t]; k++) out_ent[w++] = sort_index[ent[k]];
+}
+
+struct ScalarsReset {
+    static void eps(Scalars &s) {
+        s.eps_max   = 0;
+        s.eps_min   = ~0ull;
+        s.iters_max = 0;
+    }
+};
+
+__global__ void k_reset_eps(Scalars *sc) {
+    sc->eps_max   = 0;
+    sc->eps_min   = ~0ull;
+    sc->iters_max = 0;
+}
+__global__ void k_reset_corrector(Scalars *sc) {
+    sc->epsv2_max = 0;
+    sc->dt_min    = ~0ull;
+    sc->sum_v2    = 0;
+}
+
+} // namespace
+} // namespace gbsph
+
+using namespace gbsph;
+
+static int fail(gbsph_ctx *ctx, int code, const std::string &msg) {
+    ctx->c.err         = msg;
+    ctx->c.last_status = code;
+    return code;
+}
+
+#define CU(expr)                                                                                  \
+    do {                                                                                          \
+        cudaError_t _e = (expr);                                                                  \
+        if (_e != cudaSuccess) {                                                                  \
+            std::string _m = std::string(#expr) + ": " + cudaGetErrorString(_e);                  \
+            if (!ctx->c.err.empty()) _m += " (" + ctx->c.err + ")";                               \
+            return fail(ctx, GBSPH_ERR_CUDA, _m);                                                 \
+        }                                                                                         \
+    } while (0)
+
+#define REQUIRE_ARG(cond, msg)                                                                    \
+    do {                                                                                          \
+        if (!(cond)) return fail(ctx, GBSPH_ERR_ARG, msg);                                        \
+    } while (0)
+
+// Select the device and stream for this call; a stream switch drains the old one so
+// the stream-ordered scratch allocations are safe to reuse.
+static int enter(gbsph_ctx *ctx, void *stream) {
+    if (!ctx) return GBSPH_ERR_ARG;
+    ctx->c.err.clear();
+    cudaError_t e = cudaSetDevice(ctx->c.device);
+    if (e != cudaSuccess) return fail(ctx, GBSPH_ERR_CUDA, cudaGetErrorString(e));
+    cudaStream_t s = (cudaStream_t) stream;
+    if (s != ctx->c.stream) {
+        cudaStreamSynchronize(ctx->c.stream);
+        ctx->c.stream = s;
+    }
+    return GBSPH_OK;
+}
+#define ENTER(ctx, stream)                                                                        \
+    do {                                                                                          \
+        int _r = enter((ctx), (stream));                                                          \
+        if (_r) return _r;                                                                        \
+    } while (0)
+
+extern "C" {
+
+const char *gbsph_version(void) { return "gbsph 0.1 (sm_103a)"; }
+
+static const char *kProfNames[kProfCount] = {
+    "predict", "ghosts", "merge_bbox", "morton_sort", "tree", "leaf_lists", "owner",
+    "cache_count", "cache_fill", "h_iterate", "omega", "gather_eos", "derivs"};
+
+uint32_t gbsph_profile_kinds(void) { return kProfCount; }
+
+uint64_t gbsph_kernel_launches(void) { return g_kernel_launches; }
+
+const char *gbsph_profile_name(uint32_t kind) {
+    return kind < kProfCount ? kProfNames[kind] : "";
+}
+
+int gbsph_profile_enable(gbsph_ctx *ctx, int on) {
+    if (!ctx) return GBSPH_ERR_ARG;
+    Prof &p = ctx->c.prof;
+    cudaStreamSynchronize(ctx->c.stream);
+    p.on   = on != 0;
+    p.used = 0;
+    for (int k = 0; k < kProfCount; k++) {
+        p.ms[k]       = 0;
+        p.launches[k] = 0;
+        p.units[k]    = 0;
+    }
+    return GBSPH_OK;
+}
+
+int gbsph_profile_read(gbsph_ctx *ctx, double *ms_host, uint64_t *launches_host,
+                       uint64_t *units_host, uint32_t n) {
+    if (!ctx) return GBSPH_ERR_ARG;
+    cudaStreamSynchronize(ctx->c.stream);
+    prof_collect(ctx->c);
+    for (uint32_t k = 0; k < n && k < (uint32_t) kProfCount; k++) {
+        if (ms_host) ms_host[k] = ctx->c.prof.ms[k];
+        if (launches_host) launches_host[k] = ctx->c.prof.launches[k];
+        if (units_host) units_host[k] = ctx->c.prof.units[k];
+    }
+    return GBSPH_OK;
+}
+
+int gbsph_create(gbsph_ctx **out, int device) {
+    if (!out) return GBSPH_ERR_ARG;
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return GBSPH_ERR_CUDA;
+    gbsph_ctx *ctx = new gbsph_ctx();
+    ctx->c.device  = device;
+    ctx->c.stream  = 0;
+    if (cudaMallocHost(&ctx->c.h_scalars, sizeof(Scalars)) != cudaSuccess ||
+        ctx->c.d_scalars.ensure(sizeof(Scalars), 0) != cudaSuccess ||
+        ctx->c.d_bbox.ensure(sizeof(BBox), 0) != cudaSuccess) {
+        delete ctx;
+        return GBSPH_ERR_CUDA;
+    }
+    cudaMemsetAsync(ctx->c.d_scalars.p, 0, sizeof(Scalars), 0);
+    cudaStreamSynchronize(0);
+    *out = ctx;
+    return GBSPH_OK;
+}
+
+void gbsph_destroy(gbsph_ctx *ctx) {
+    if (ctx) delete ctx;
+}
+
+const char *gbsph_last_error(const gbsph_ctx *ctx) { return ctx ? ctx->c.err.c_str() : "null context"; }
+
+int gbsph_morton_codes(gbsph_ctx *ctx, const double *x, const double *y, const double *z,
+                       uint32_t n, uint32_t morton_count, const double bmin_host[3],
+                       const double bmax_host[3], int key_bits, void *keys_out, void *stream) {
+    ENTER(ctx, stream);
+    REQUIRE_ARG(morton_count >= n, "MortonCodeSet: morton_count < cnt_obj");
+    REQUIRE_ARG(key_bits == 32 || key_bits == 64, "key_bits must be 32 or 64");
+    CU(set_bbox_host(ctx->c, bmin_host, bmax_host));
+    CU(morton_codes_dev(ctx->c, x, y, z, n, morton_count, key_bits, keys_out));
+    return GBSPH_OK;
+}
+
+int gbsph_sort_by_key(gbsph_ctx *ctx, void *keys, uint32_t *vals, uint32_t len, int key_bits,
+                      void *stream) {
+    ENTER(ctx, stream);
+    REQUIRE_ARG(len == 0 || (len & (len - 1)) == 0,
+                "this algorithm can only be used with length that are powers of two");
+    if (key_bits == 64) CU(sort_keys_dev<u64>((u64 *) keys, vals, len, ctx->c.stream));
+    else CU(sort_keys_dev<u32>((u32 *) keys, vals, len, ctx->c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_build_tree(gbsph_ctx *ctx, const double *x, const double *y, const double *z,
+                     const double *h, uint32_t n, const double bmin_host[3],
+                     const double bmax_host[3], uint32_t reduction_level, double htol,
+                     int key_bits, uint32_t morton_count, void *stream) {
+    ENTER(ctx, stream);
+    REQUIRE_ARG(n > 0, "obj_cnt is 0, cannot build a CompressedLeafBVH");
+    REQUIRE_ARG(key_bits == 32 || key_bits == 64, "key_bits must be 32 or 64");
+    REQUIRE_ARG(morton_count == 0 || (morton_count >= n && (morton_count & (morton_count - 1)) == 0),
+                "morton_count must be 0 or a power of two >= n");
+    CU(cudaMemsetAsync(ctx->c.d_scalars.p, 0, sizeof(Scalars), ctx->c.stream));
+    CU(set_bbox_host(ctx->c, bmin_host, bmax_host));
+    CU(tree_build(ctx->c, x, y, z, h, n, reduction_level, htol, key_bits, morton_count));
+    ctx->c.cache_valid = false;
+    CU(cudaStreamSynchronize(ctx->c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_tree_counts(gbsph_ctx *ctx, uint32_t *mc, uint32_t *lc) {
+    if (!ctx) return GBSPH_ERR_ARG;
+    if (mc) *mc = ctx->c.morton_count;
+    if (lc) *lc = ctx->c.leaf_count;
+    return GBSPH_OK;
+}
+
+int gbsph_tree_export(gbsph_ctx *ctx, void *sorted_keys, uint32_t *sort_index, uint32_t *reduc,
+                      void *reduced_keys, uint32_t *lchild, uint32_t *rchild, uint8_t *lflag,
+                      uint8_t *rflag, uint32_t *endrange, double *aabb_min, double *aabb_max,
+                      double *rint, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(c.leaf_count > 0, "no tree built");
+    size_t ks = c.key_bits / 8;
+    u32 P = c.morton_count, L = c.leaf_count, I = L - 1;
+    cudaStream_t s = c.stream;
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        return (dst && bytes) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s)
+                              : cudaSuccess;
+    };
+    CU(cp(sorted_keys, c.keys.p, ks * P));
+    CU(cp(sort_index, c.sort_index.p, 4 * (size_t) P));
+    CU(cp(reduc, c.reduc.p, 4 * ((size_t) L + 2)));
+    CU(cp(reduced_keys, c.reduced.p, ks * L));
+    CU(cp(lchild, c.lchild.p, 4 * (size_t) I));
+    CU(cp(rchild, c.rchild.p, 4 * (size_t) I));
+    CU(cp(lflag, c.lflag.p, I));
+    CU(cp(rflag, c.rflag.p, I));
+    CU(cp(endrange, c.endrange.p, 4 * (size_t) I));
+    if (aabb_min || aabb_max || rint) CU(export_boxes(c, aabb_min, aabb_max, rint));
+    CU(cudaStreamSynchronize(s));
+    return GBSPH_OK;
+}
+
+int gbsph_tree_query(gbsph_ctx *ctx, const double *qx, const double *qy, const double *qz,
+                     uint32_t nq, int mode, double s, uint32_t *counts, uint32_t *out,
+                     uint64_t capacity, uint64_t *total_host, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(c.leaf_count > 0, "no tree built");
+    REQUIRE_ARG(counts != nullptr, "counts required");
+    CU(cudaMemsetAsync(c.d_scalars.p, 0, sizeof(Scalars), c.stream));
+    CU(tree_query(c, qx, qy, qz, nq, mode, s, counts, nullptr, nullptr, false));
+    CU(c.offsets.ensure(sizeof(u32) * ((size_t) nq + 1), c.stream));
+    CU(scan_exclusive_u32(counts, c.offsets.as<u32>(), nq, &c.d_scalars.as<Scalars>()->total,
+                          c.scan_scratch, c.stream));
+    CU(sync_scalars(c));
+    u64 total = c.h_scalars->total;
+    if (total_host) *total_host = total;
+    if (out && capacity >= total) {
+        CU(tree_query(c, qx, qy, qz, nq, mode, s, nullptr, c.offsets.as<u32>(), out, true));
+        CU(cudaStreamSynchronize(c.stream));
+    } else if (out) {
+        return fail(ctx, GBSPH_ERR_CAPACITY, "tree_query: output capacity too small");
+    }
+    return GBSPH_OK;
+}
+
+int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    if (c.leaf_count == 0 || !c.has_rint || c.key_bits != 32)
+        return fail(ctx, GBSPH_ERR_STATE, "neighbour cache needs a 32-bit tree built with h");
+    REQUIRE_ARG(n_local <= c.n_obj, "n_local > merged count");
+    CU(cudaMemsetAsync(c.d_scalars.p, 0, sizeof(Scalars), c.stream));
+    CU(build_rows(c, n_local));
+    CU(neigh_cache_build(c, htol));
+    CU(cudaStreamSynchronize(c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_cache_size(gbsph_ctx *ctx, uint64_t *total, uint64_t *leaf_total) {
+    if (!ctx) return GBSPH_ERR_ARG;
+    if (total) *total = ctx->c.csr_total;
+    if (leaf_total) *leaf_total = ctx->c.leaf_csr_total;
+    return GBSPH_OK;
+}
+
+int gbsph_cache_export(gbsph_ctx *ctx, uint32_t *cnt, uint32_t *scanned, uint32_t *entries,
+                       void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    if (!c.cache_valid) return fail(ctx, GBSPH_ERR_STATE, "no neighbour cache built");
+    REQUIRE_ARG(cnt && scanned, "cnt and scanned required");
+    u32 n = c.n_local;
+    { k_cache_export_counts<<<div_up(n, 256), 256, 0, c.stream>>>(n, c.row_local.as<u32>(),
+                                                                c.csr_cnt.as<u32>(), cnt); GBSPH_COUNTED; }
+    CU(cudaGetLastError());
+    CU(scan_exclusive_u32(cnt, scanned, n, &c.d_scalars.as<Scalars>()->total2, c.scan_scratch,
+                          c.stream));
+    if (entries)
+        { k_cache_export_entries<<<div_up(n, 256), 256, 0, c.stream>>>(
+            n, c.row_local.as<u32>(), c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
+            c.sort_index.as<u32>(), scanned, entries); GBSPH_COUNTED; }
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_h_iterate(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
+                    const uint32_t *entries, const double *x, const double *y, const double *z,
+                    const double *h_old, double *h_new, double *eps, uint32_t n_local,
+                    double pmass, double h_evol_max, double h_evol_iter_max, uint32_t iters,
+                    double *max_eps_host, double *min_eps_host, uint32_t *iters_used_host,
+                    void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(iters >= 1, "iters >= 1");
+    RowSpace rs{n_local, nullptr, nullptr, cnt, scanned, entries, x, y, z};
+    { k_reset_eps<<<1, 1, 0, c.stream>>>(c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    CU(h_iterate64(c, rs, h_old, h_new, eps, pmass, h_evol_max, h_evol_iter_max, iters));
+    CU(sync_scalars(c));
+    if (max_eps_host) *max_eps_host = ordered_to_f64(c.h_scalars->eps_max);
+    if (min_eps_host) *min_eps_host = ordered_to_f64(c.h_scalars->eps_min);
+    if (iters_used_host) *iters_used_host = c.h_scalars->iters_max;
+    return GBSPH_OK;
+}
+
+int gbsph_omega(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
+                const uint32_t *entries, const double *x, const double *y, const double *z,
+                const double *h, uint32_t n_local, double pmass, double *omega, void *stream) {
+    ENTER(ctx, stream);
+    RowSpace rs{n_local, nullptr, nullptr, cnt, scanned, entries, x, y, z};
+    CU(omega64(ctx->c, rs, h, pmass, omega, nullptr));
+    CU(cudaStreamSynchronize(ctx->c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_eos_adiabatic(gbsph_ctx *ctx, const double *h, const double *u, uint32_t n, double pmass,
+                        double gamma, double *P, double *cs, void *stream) {
+    ENTER(ctx, stream);
+    CU(eos64(ctx->c, n, h, u, pmass, gamma, P, cs));
+    CU(cudaStreamSynchronize(ctx->c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
+                         const uint32_t *entries, const double *x, const double *y,
+                         const double *z, const double *vx, const double *vy, const double *vz,
+                         const double *h, const double *omega, const double *u, const double *P,
+                         const double *cs, uint32_t n_local, uint32_t n_merged, double pmass,
+                         double alpha_u, double alpha_AV, double beta_AV, uint32_t precision,
+                         double *ax, double *ay, double *az, double *du, double *vsig,
+                         void *stream) {
+    ENTER(ctx, stream);
+    REQUIRE_ARG(n_merged >= n_local, "n_merged < n_local");
+    ctx->c.n_obj = n_merged;
+    RowSpace rs{n_local, nullptr, nullptr, cnt, scanned, entries, x, y, z};
+    HydroSpace hs{h, u, vx, vy, vz, omega, P, cs};
+    if (precision == GBSPH_MIXED) {
+        CU(derivs_mixed_module(ctx->c, rs, hs, pmass, alpha_u, alpha_AV, beta_AV, ax, ay, az, du,
+                               vsig));
+    } else {
+        REQUIRE_ARG(precision == GBSPH_FP64, "unknown precision");
+        CU(derivs64(ctx->c, rs, hs, pmass, alpha_u, alpha_AV, beta_AV, ax, ay, az, du, vsig));
+    }
+    CU(cudaStreamSynchronize(ctx->c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_periodic_ghosts(gbsph_ctx *ctx, gbsph_vec3 xyz, const double *h, uint32_t n_local,
+                          const double bmin_host[3], const double bmax_host[3], double htol,
+                          uint32_t *n_ghost_host, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(n_local > 0, "empty patch");
+    CU(periodic_ghosts(c, xyz.x, xyz.y, xyz.z, xyz.stride, h, n_local, bmin_host, bmax_host, htol));
+    CU(merge_positions(c, xyz.x, xyz.y, xyz.z, xyz.stride, h, n_local));
+    CU(cudaStreamSynchronize(c.stream));
+    c.n_local = n_local;
+    if (n_ghost_host) *n_ghost_host = c.n_ghost;
+    return GBSPH_OK;
+}
+
+int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double *mx, double *my,
+                       double *mz, double *mh, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    u32 G = c.n_ghost, N = c.n_local + c.n_ghost;
+    cudaStream_t s = c.stream;
+    if (src && G) CU(cudaMemcpyAsync(src, c.ghost_src.p, 4 * (size_t) G, cudaMemcpyDeviceToDevice, s));
+    if (offset_id && G) CU(cudaMemcpyAsync(offset_id, c.ghost_oid.p, G, cudaMemcpyDeviceToDevice, s));
+    if (mx) CU(cudaMemcpyAsync(mx, c.mx.p, 8 * (size_t) N, cudaMemcpyDeviceToDevice, s));
+    if (my) CU(cudaMemcpyAsync(my, c.my.p, 8 * (size_t) N, cudaMemcpyDeviceToDevice, s));
+    if (mz) CU(cudaMemcpyAsync(mz, c.mz.p, 8 * (size_t) N, cudaMemcpyDeviceToDevice, s));
+    if (mh) CU(cudaMemcpyAsync(mh, c.mh.p, 8 * (size_t) N, cudaMemcpyDeviceToDevice, s));
+    CU(cudaStreamSynchronize(s));
+    return GBSPH_OK;
+}
+
+int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
+                      gbsph_time_state *ts, gbsph_step_log *log, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(p && cfg && ts, "null argument");
+    REQUIRE_ARG(p->n > 0, "empty patch");
+    REQUIRE_ARG(cfg->pmass > 0,
+                "invalid gpart_mass, this configuration can not converge (Solver.cpp:1096-1102)");
+    REQUIRE_ARG(cfg->precision == GBSPH_FP64 || cfg->precision == GBSPH_MIXED, "unknown precision");
+    REQUIRE_ARG(p->xyz.stride == p->vxyz.stride && p->xyz.stride == p->axyz.stride,
+                "xyz, vxyz and axyz must share one element stride");
+    auto t_start = std::chrono::steady_clock::now();
+    cudaStream_t s = c.stream;
+    const u32 n    = p->n;
+    const f64 dt   = ts->dt;
+    const bool mixed = cfg->precision == GBSPH_MIXED;
+    LocalFields lf{p->xyz.x,  p->xyz.y,  p->xyz.z,  p->vxyz.x, p->vxyz.y,  p->vxyz.z,
+                   p->axyz.x, p->axyz.y, p->axyz.z, p->xyz.stride, p->hpart, p->uint, p->duint};
+    gbsph_step_log lg;
+    std::memset(&lg, 0, sizeof(lg));
+    lg.t       = ts->t;
+    lg.dt      = dt;
+    lg.n_local = n;
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    CU(cudaMemsetAsync(dsc, 0, sizeof(Scalars), s));
+
+    // ---- leapfrog predictor + position boundary
+    CU(predict64(c, lf, n, dt, (int) cfg->periodic, cfg->box_min, cfg->box_max));
+
+    // ---- sph_prestep (Solver.cpp:1060-1304)
+    CU(c.h_old_row.ensure(8 * (size_t) n, s));
+    CU(c.hnew_row.ensure(8 * (size_t) n, s));
+    CU(c.eps_row.ensure(8 * (size_t) n, s));
+    CU(c.omega_local.ensure(8 * (size_t) n, s));
+    const bool fused_h = cfg->epsilon_h <= 1e-6;
+    u32 hstep = 0;
+    f64 max_eps = 0, min_eps = 0;
+    bool converged = false;
+    RowSpace rs{};
+    for (; hstep < cfg->h_max_subcycles; hstep++) {
+        if (cfg->periodic) {
+            CU(periodic_ghosts(c, lf.x, lf.y, lf.z, lf.vs, lf.h, n, cfg->box_min, cfg->box_max,
+                               cfg->htol_up_coarse));
+        } else {
+            c.n_ghost = 0;
+        }
+        CU(merge_positions(c, lf.x, lf.y, lf.z, lf.vs, lf.h, n));
+        u32 N = n + c.n_ghost;
+        CU(bbox_from_merged(c, N));
+        CU(tree_build(c, c.mx.as<f64>(), c.my.as<f64>(), c.mz.as<f64>(), c.mh.as<f64>(), N,
+                      cfg->tree_reduction_level, cfg->htol_up_coarse, 32, 0));
+        CU(build_rows(c, n));
+        CU(neigh_cache_build(c, cfg->htol_up_coarse));
+        if (mixed) CU(stage_positions_mixed(c, N));
+        rs = RowSpace{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
+                      c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
+                      c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
+        CU(gather_rows(c, n, c.sh.as<f64>(), c.h_old_row.as<f64>(), c.hnew_row.as<f64>()));
+        CU(fill64(c, n, c.eps_row.as<f64>(), 100.0));
+        u32 iters_total = 0;
+        if (fused_h) {
+            { k_reset_eps<<<1, 1, 0, s>>>(dsc); GBSPH_COUNTED; }
+            if (mixed)
+                CU(h_iterate_mixed(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
+                                   c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
+                                   cfg->htol_up_fine, cfg->h_iter_per_subcycles));
+            else
+                CU(h_iterate64(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
+                               c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
+                               cfg->htol_up_fine, cfg->h_iter_per_subcycles));
+            CU(sync_scalars(c));
+            max_eps     = ordered_to_f64(c.h_scalars->eps_max);
+            min_eps     = ordered_to_f64(c.h_scalars->eps_min);
+            iters_total = c.h_scalars->iters_max;
+        } else {
+            for (u32 it = 0; it < cfg->h_iter_per_subcycles; it++) {
+                { k_reset_eps<<<1, 1, 0, s>>>(dsc); GBSPH_COUNTED; }
+                if (mixed)
+                    CU(h_iterate_mixed(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
+                                       c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
+                                       cfg->htol_up_fine, 1));
+                else
+                    CU(h_iterate64(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
+                                   c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
+                                   cfg->htol_up_fine, 1));
+                CU(sync_scalars(c));
+                max_eps = ordered_to_f64(c.h_scalars->eps_max);
+                min_eps = ordered_to_f64(c.h_scalars->eps_min);
+                iters_total++;
+                if (max_eps < cfg->epsilon_h) break;
+            }
+        }
+        lg.h_iterations += iters_total;
+        // the iterated h is written back whether or not the sub-cycle converged
+        CU(scatter_rows(c, n, c.hnew_row.as<f64>(), lf.h));
+        converged = (max_eps < cfg->epsilon_h) && !(min_eps < 0);
+        if (converged) break;
+    }
+    // hstep + 1 sub-cycles ran; h_max_subcycles + 1 flags "never converged", after which
+    // the reference logs an error and carries on with the step (Solver.cpp:1271-1273)
+    lg.h_subcycles = hstep + 1;
+    lg.max_eps_h   = max_eps;
+    lg.n_ghost     = c.n_ghost;
+    lg.leaf_count  = c.leaf_count;
+    lg.cache_size  = c.csr_total;
+    u32 N          = n + c.n_ghost;
+    if (mixed) CU(omega_mixed(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>()));
+    else CU(omega64(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>(),
+                    c.row_local.as<u32>()));
+    if (p->omega)
+        CU(cudaMemcpyAsync(p->omega, c.omega_local.p, 8 * (size_t) n, cudaMemcpyDeviceToDevice, s));
+
+    // ---- corrector loop (Solver.cpp:2247-3171)
+    DevBuf *rank_bufs[] = {&c.sh2, &c.su, &c.svx, &c.svy, &c.svz, &c.som, &c.sP, &c.scs};
+    for (DevBuf *b : rank_bufs) CU(b->ensure(8 * (size_t) N, s));
+    HydroSpace hs{c.sh2.as<f64>(), c.su.as<f64>(),  c.svx.as<f64>(), c.svy.as<f64>(),
+                  c.svz.as<f64>(), c.som.as<f64>(), c.sP.as<f64>(),  c.scs.as<f64>()};
+    f64 next_cfl   = 0;
+    bool rerun     = false;
+    u32 corr_iters = 0;
+    do {
+        if (corr_iters == 50)
+            return fail(ctx, GBSPH_ERR_NOT_CONVERGED,
+                        "the corrector has made over 50 loops, either their is a bug, either you "
+                        "are using a dt that is too large");
+        CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, cfg->gamma));
+        { k_reset_corrector<<<1, 1, 0, s>>>(dsc); GBSPH_COUNTED; }
+        f64 C_cour  = cfg->cfl_cour * ts->cfl_mult;
+        f64 C_force = cfg->cfl_force * ts->cfl_mult;
+        if (mixed)
+            CU(derivs_step_mixed(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
+                                 dt / 2, C_cour, C_force, lf));
+        else
+            CU(derivs_step64(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
+                             dt / 2, C_cour, C_force, lf));
+        CU(sync_scalars(c));
+        f64 rank_veps_v = std::sqrt(ordered_to_f64(c.h_scalars->epsv2_max));
+        f64 vmean       = std::sqrt(c.h_scalars->sum_v2 / f64(n));
+        f64 eps_v       = rank_veps_v / vmean;
+        if (vmean <= 0) eps_v = 0;
+        lg.eps_v = eps_v;
+        if (eps_v > 1e-2) {
+            rerun        = true;
+            ts->cfl_mult = ts->cfl_mult / 2;
+        } else {
+            rerun    = false;
+            next_cfl = ordered_to_f64(c.h_scalars->dt_min);
+        }
+        corr_iters++;
+    } while (rerun);
+    if (c.h_scalars->flags)
+        return fail(ctx, GBSPH_ERR_CUDA, "kernel error flags raised during the step");
+
+    auto t_end    = std::chrono::steady_clock::now();
+    f64 elapsed   = std::chrono::duration<f64>(t_end - t_start).count();
+    lg.corrector_iters = corr_iters;
+    ts->dt             = next_cfl;
+    ts->t              = ts->t + dt;
+    f64 stiff          = cfg->cfl_mult_stiffness;
+    ts->cfl_mult       = (ts->cfl_mult * stiff + 1.) / (stiff + 1.);
+    lg.next_dt         = ts->dt;
+    lg.cfl_mult        = ts->cfl_mult;
+    lg.elapsed_s       = elapsed;
+    lg.rate            = elapsed > 0 ? f64(n) / elapsed : 0;
+    if (log) *log = lg;
+    if (!converged) ctx->c.err = "the h iterator is not converged after the maximum number of "
+                                 "sub-cycles (step continued, as the reference does)";
+    return GBSPH_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,164 @@
+// Library context: the scratch arena behind the C ABI.  One context serves one
+// host thread and one stream at a time (the same contract as the reference's
+// per-rank compute queue).  All buffers grow on demand and are reused across steps.
+#pragma once
+
+#include "gbsph_internal.cuh"
+
+#include <string>
+#include <vector>
+
+namespace gbsph {
+
+// Widened bounding box of the merged positions and the Morton grid step
+// (BuildTrees.cpp:26-59, CoordRangeTransform.cpp:169-184).
+struct BBox {
+    f64 lo[3];
+    f64 hi[3];
+    f64 fact[3];
+};
+
+// Small device-side reduction results, read back through pinned memory.
+struct Scalars {
+    u64 bbox_min[3];   // ordered-u64 min of merged positions
+    u64 bbox_max[3];   // ordered-u64 max
+    u64 hmax;          // ordered-u64 max of local h
+    u64 eps_max;       // ordered-u64 max of eps_h (h iteration)
+    u64 eps_min;       // ordered-u64 min of eps_h
+    u64 epsv2_max;     // ordered-u64 max of |dv corrector|^2
+    u64 dt_min;        // ordered-u64 min of per-particle CFL dt
+    u64 n_unconverged; // particles whose per-thread iteration cap was hit
+    f64 sum_v2;        // sum of |v|^2 after the corrector
+    f64 cons[8];       // conservation totals (momentum, energies)
+    u32 total;         // scan totals
+    u32 total2;
+    u32 ghost_total;
+    u32 iters_max;     // max Newton iterations used by any particle
+    u32 flags;         // error flags raised by kernels
+    u32 pad;
+};
+
+enum KernelFlags : u32 {
+    kFlagStackOverflow = 1u,
+    kFlagOwnerMissing  = 2u,
+    kFlagCsrOverflow   = 4u,
+};
+
+// Live per-stage timing with CUDA events on the launching stream (off by default).
+enum ProfKind : int {
+    kProfPredict = 0,
+    kProfGhosts,
+    kProfMerge,
+    kProfSort,
+    kProfTree,
+    kProfStage1,
+    kProfOwner,
+    kProfCacheCount,
+    kProfCacheFill,
+    kProfHIter,
+    kProfOmega,
+    kProfGatherEos,
+    kProfDerivs,
+    kProfCount
+};
+
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool; // start/stop pairs
+    std::vector<int> kinds;
+    size_t used = 0;
+    double ms[kProfCount]       = {};
+    u64 launches[kProfCount]    = {};
+    u64 units[kProfCount]       = {};
+};
+
+struct Ctx {
+    Prof prof;
+    int device          = 0;
+    cudaStream_t stream = 0;
+    std::string err;
+    int last_status = 0;
+
+    DevBuf scan_scratch;
+    DevBuf d_scalars; // Scalars
+    Scalars *h_scalars = nullptr; // pinned mirror
+    DevBuf d_bbox;    // BBox
+
+    // ---- tree (CompressedLeafBVH) over the merged set
+    int key_bits = 32;
+    u32 n_obj = 0, morton_count = 0, leaf_count = 0;
+    DevBuf keys, sort_index, flags_a, flags_b, offsets, reduc, reduced;
+    DevBuf lchild, rchild, lflag, rflag, endrange, parent, boxes, visit;
+    bool has_rint = false;
+
+    // ---- rank-ordered copies of merged fields
+    DevBuf rank_of;            // merged id -> rank
+    DevBuf sx, sy, sz, sh;     // positions, h (tree build time)
+    DevBuf row_rank, row_local; // local rows in rank order
+    DevBuf row_flags, row_offsets;
+
+    // ---- neighbour cache
+    u64 leaf_csr_total = 0, csr_total = 0;
+    DevBuf leaf_cnt, leaf_off, leaf_ent; // stage 1 (leaf ids)
+    DevBuf owner;                        // per row: leaf index
+    DevBuf csr_cnt, csr_off, csr_ent;    // stage 2, per row, entries are ranks
+    u32 n_local = 0;
+    bool cache_valid = false;
+
+    // ---- ghosts
+    u32 n_ghost = 0;
+    DevBuf ghost_src, ghost_oid;  // source local id, offset index (0..25)
+    DevBuf ghost_block_counts;    // per block x 26
+    DevBuf mx, my, mz, mh;        // merged positions / h (merged id order)
+    f64 ghost_offsets[26][3];
+    DevBuf d_ghost_offsets;       // f64[26][3]
+
+    // ---- per-step fields in rank order (corrector phase)
+    DevBuf su, svx, svy, svz, som, sP, scs, sh2;
+    // mixed precision staging (rank order)
+    DevBuf f_pos, f_anchor, f_aux0, f_aux1, f_aux2;
+
+    // ---- per-row / per-local work arrays
+    DevBuf h_old_row, eps_row, omega_local, a_old, du_old, hnew_row, omega_row;
+    DevBuf dt_part;
+
+    ~Ctx();
+};
+
+// ------------------------------------------------------------------ profiling
+int prof_begin(Ctx &c, int kind, u64 units);
+void prof_end(Ctx &c, int idx);
+void prof_collect(Ctx &c); // after a stream sync: fold recorded pairs into the totals
+
+struct ProfScope {
+    Ctx &c;
+    int idx;
+    ProfScope(Ctx &c_, int kind, u64 units) : c(c_), idx(c_.prof.on ? prof_begin(c_, kind, units) : -1) {}
+    ~ProfScope() {
+        if (idx >= 0) prof_end(c, idx);
+    }
+};
+
+// ------------------------------------------------------------------ stage functions
+// All return cudaError_t and enqueue work on ctx.stream.
+
+// tree.cu
+cudaError_t tree_build(Ctx &c, const f64 *x, const f64 *y, const f64 *z, const f64 *h, u32 n,
+                       u32 level, f64 htol, int key_bits, u32 morton_count);
+cudaError_t set_bbox_host(Ctx &c, const f64 *bmin, const f64 *bmax);
+cudaError_t bbox_from_merged(Ctx &c, u32 n); // reduce mx/my/mz -> widened d_bbox
+cudaError_t sync_scalars(Ctx &c);            // copy Scalars to pinned host, wait
+
+// neigh.cu
+cudaError_t build_rows(Ctx &c, u32 n_local);
+cudaError_t neigh_cache_build(Ctx &c, f64 h_tolerance);
+cudaError_t tree_query(Ctx &c, const f64 *qx, const f64 *qy, const f64 *qz, u32 nq, int mode,
+                       f64 s, u32 *counts, u32 *offsets, u32 *out, bool fill);
+
+// ghosts.cu
+cudaError_t periodic_ghosts(Ctx &c, const f64 *x, const f64 *y, const f64 *z, u32 vs,
+                            const f64 *h, u32 n, const f64 *bmin, const f64 *bmax, f64 htol);
+cudaError_t merge_positions(Ctx &c, const f64 *x, const f64 *y, const f64 *z, u32 vs,
+                            const f64 *h, u32 n);
+
+} // namespace gbsph

@@ -1,0 +1,355 @@
+// Two-stage neighbour cache over the compressed-leaf BVH —
+//   shammodels/sph/src/modules/NeighbourCache.cpp:223-596 (start_neighbors_cache_2stages),
+//   traversal shamtree/include/shamtree/KarrasTreeTraverser.hpp:70-118 (left-first DFS),
+//   criteria shamtree/include/shamtree/kernels/geometry_utils.hpp:62-135,
+//   CSR layout shamtree/include/shamtree/TreeTraversal.hpp:375-526.
+//
+// Stage 1: leaf -> candidate leaves (extended-AABB overlap, both directions).
+// Owner:   local particle -> leaf (the last leaf, in DFS order, whose box holds it).
+// Stage 2: local particle -> interacting particles, pair test
+//          !(r^2 > (h_a htol)^2 R^2 && r^2 > (h_b htol)^2 R^2).
+// Rows are local particles in Morton order; entries are ranks, so a row lists its
+// neighbours in exactly the reference order (ascending leaf, then in-leaf order).
+
+#include "gbsph_ctx.cuh"
+
+namespace gbsph {
+
+namespace {
+
+constexpr int kStack = 64;
+
+__device__ __forceinline__ void load_box(const NodeBox *__restrict__ b, f64 lo[3], f64 hi[3],
+                                         f64 &rint) {
+    const double2 *p = (const double2 *) b;
+    double2 a = __ldg(p), c = __ldg(p + 1), d = __ldg(p + 2), e = __ldg(p + 3);
+    lo[0] = a.x;
+    lo[1] = a.y;
+    lo[2] = c.x;
+    rint  = c.y;
+    hi[0] = d.x;
+    hi[1] = d.y;
+    hi[2] = e.x;
+}
+
+struct TreeView {
+    const u32 *lchild, *rchild;
+    const u8 *lflag, *rflag;
+    const NodeBox *boxes;
+    const u32 *reduc;
+    u32 L;
+    __device__ u32 off() const { return L - 1; }
+    __device__ u32 left(u32 n) const { return lchild[n] + off() * (u32) lflag[n]; }
+    __device__ u32 right(u32 n) const { return rchild[n] + off() * (u32) rflag[n]; }
+};
+
+// left-first stack DFS; on_leaf(leaf_index) in ascending leaf order
+template<class Crit, class OnLeaf>
+__device__ __forceinline__ bool dfs(const TreeView &t, Crit &&crit, OnLeaf &&on_leaf) {
+    u32 stack[kStack];
+    int top      = 0;
+    stack[top++] = 0;
+    u32 off      = t.off();
+    while (top > 0) {
+        u32 node = stack[--top];
+        if (!crit(node)) continue;
+        if (node >= off) {
+            on_leaf(node - off);
+        } else {
+            if (top + 2 > kStack) return false;
+            stack[top++] = t.right(node);
+            stack[top++] = t.left(node);
+        }
+    }
+    return true;
+}
+
+// ---- stage 1 criterion (NeighbourCache.cpp:289-334)
+__device__ __forceinline__ bool cella_neigh_b(const f64 amin[3], const f64 amax[3],
+                                              const f64 bmin[3], const f64 bmax[3]) {
+    return (fmax(amin[0], bmin[0]) <= fmin(amax[0], bmax[0]))
+           && (fmax(amin[1], bmin[1]) <= fmin(amax[1], bmax[1]))
+           && (fmax(amin[2], bmin[2]) <= fmin(amax[2], bmax[2]));
+}
+
+struct LeafCrit {
+    const TreeView &t;
+    f64 amin[3], amax[3], amin_ext[3], amax_ext[3];
+    __device__ LeafCrit(const TreeView &tv, u32 leaf) : t(tv) {
+        f64 r;
+        load_box(&t.boxes[t.off() + leaf], amin, amax, r);
+        f64 ra = __dmul_rn(r, kRkern);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            amin_ext[c] = __dsub_rn(amin[c], ra);
+            amax_ext[c] = __dadd_rn(amax[c], ra);
+        }
+    }
+    __device__ bool operator()(u32 node) const {
+        f64 nlo[3], nhi[3], r;
+        load_box(&t.boxes[node], nlo, nhi, r);
+        f64 rn = __dmul_rn(r, kRkern);
+        f64 emin[3], emax[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            emin[c] = __dsub_rn(nlo[c], rn);
+            emax[c] = __dadd_rn(nhi[c], rn);
+        }
+        return cella_neigh_b(amin, amax, emin, emax) || cella_neigh_b(amin_ext, amax_ext, nlo, nhi);
+    }
+};
+
+__global__ void k_leaf_count(TreeView t, u32 *__restrict__ cnt, u32 *__restrict__ flags) {
+    u32 l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= t.L) return;
+    LeafCrit crit(t, l);
+    u32 c   = 0;
+    bool ok = dfs(t, crit, [&](u32) { c++; });
+    if (!ok) atomicOr(flags, kFlagStackOverflow);
+    cnt[l] = c;
+}
+
+__global__ void k_leaf_fill(TreeView t, const u32 *__restrict__ off, u32 *__restrict__ ent) {
+    u32 l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= t.L) return;
+    LeafCrit crit(t, l);
+    u32 w = off[l];
+    dfs(t, crit, [&](u32 leaf) { ent[w++] = leaf; });
+}
+
+// ---- rows: local particles in rank order
+__global__ void k_row_flags(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
+                            u8 *__restrict__ flags) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    flags[r] = sort_index[r] < n_local ? 1 : 0;
+}
+__global__ void k_rows(const u32 *__restrict__ sort_index, const u8 *__restrict__ flags,
+                       const u32 *__restrict__ offs, u32 N, u32 *__restrict__ row_rank,
+                       u32 *__restrict__ row_local) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N || !flags[r]) return;
+    u32 row        = offs[r];
+    row_rank[row]  = r;
+    row_local[row] = sort_index[r];
+}
+
+// ---- owner leaf: max leaf index whose box contains the point (inclusive bounds),
+// i.e. the last leaf the reference's left-first DFS reports (NeighbourCache.cpp:419-443)
+__global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows,
+                        const f64 *__restrict__ sx, const f64 *__restrict__ sy,
+                        const f64 *__restrict__ sz, u32 *__restrict__ owner, u32 *__restrict__ flags) {
+    u32 row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    u32 r    = row_rank[row];
+    f64 p[3] = {sx[r], sy[r], sz[r]};
+    u32 stack[kStack];
+    int top      = 0;
+    stack[top++] = 0;
+    u32 off      = t.off();
+    u32 found    = kNone;
+    while (top > 0) {
+        u32 node = stack[--top];
+        f64 lo[3], hi[3], rr;
+        load_box(&t.boxes[node], lo, hi, rr);
+        bool in = (lo[0] <= p[0]) && (p[0] <= hi[0]) && (lo[1] <= p[1]) && (p[1] <= hi[1])
+                  && (lo[2] <= p[2]) && (p[2] <= hi[2]);
+        if (!in) continue;
+        if (node >= off) {
+            found = node - off;
+            break;
+        }
+        if (top + 2 > kStack) {
+            atomicOr(flags, kFlagStackOverflow);
+            break;
+        }
+        stack[top++] = t.left(node);
+        stack[top++] = t.right(node);
+    }
+    if (found == kNone) {
+        atomicOr(flags, kFlagOwnerMissing);
+        found = 0;
+    }
+    owner[row] = found;
+}
+
+// ---- stage 2 (NeighbourCache.cpp:492-591)
+template<bool FILL>
+__global__ void __launch_bounds__(256) k_part_cache(
+    const u32 *__restrict__ row_rank, u32 n_rows, const u32 *__restrict__ owner,
+    const u32 *__restrict__ leaf_cnt, const u32 *__restrict__ leaf_off,
+    const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const f64 *__restrict__ sx,
+    const f64 *__restrict__ sy, const f64 *__restrict__ sz, const f64 *__restrict__ sh,
+    f64 h_tol, u32 *__restrict__ cnt, const u32 *__restrict__ off, u32 *__restrict__ ent) {
+    u32 row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    u32 ra    = row_rank[row];
+    f64 xa    = sx[ra], ya = sy[ra], za = sz[ra];
+    f64 rint_a = __dmul_rn(sh[ra], h_tol);
+    f64 thr_a = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
+    u32 leaf  = owner[row];
+    u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
+    u32 c = 0, w = FILL ? off[row] : 0;
+    for (u32 k = k0; k < k1; k++) {
+        u32 lb = leaf_ent[k];
+        u32 r0 = reduc[lb], r1 = reduc[lb + 1];
+        for (u32 rb = r0; rb < r1; rb++) {
+            f64 dx = __dsub_rn(xa, sx[rb]), dy = __dsub_rn(ya, sy[rb]), dz = __dsub_rn(za, sz[rb]);
+            f64 rab2   = dot3_rn(dx, dy, dz);
+            f64 rint_b = __dmul_rn(sh[rb], h_tol);
+            f64 thr_b  = __dmul_rn(__dmul_rn(rint_b, rint_b), kRkern * kRkern);
+            bool no_interact = rab2 > thr_a && rab2 > thr_b;
+            if (!no_interact) {
+                if (FILL) ent[w++] = rb;
+                c++;
+            }
+        }
+    }
+    if (!FILL) cnt[row] = c;
+}
+
+// ---- generic object query (CLBVHObjectIterator::rtree_for, CLBVHObjectIterator.hpp:127-169)
+template<bool FILL>
+__global__ void k_query(TreeView t, const f64 *__restrict__ qx, const f64 *__restrict__ qy,
+                        const f64 *__restrict__ qz, u32 nq, int mode, f64 s,
+                        const u32 *__restrict__ sort_index, const f64 *__restrict__ sx,
+                        const f64 *__restrict__ sy, const f64 *__restrict__ sz,
+                        u32 *__restrict__ counts, const u32 *__restrict__ offs, u32 *__restrict__ out,
+                        u32 *__restrict__ flags) {
+    u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    f64 lo[3] = {__dadd_rn(qx[q], -s), __dadd_rn(qy[q], -s), __dadd_rn(qz[q], -s)};
+    f64 hi[3] = {__dadd_rn(qx[q], s), __dadd_rn(qy[q], s), __dadd_rn(qz[q], s)};
+    u32 c = 0, w = FILL ? offs[q] : 0;
+    bool ok = dfs(
+        t,
+        [&](u32 node) {
+            if (mode == 0) return true;
+            f64 nl[3], nh[3], r;
+            load_box(&t.boxes[node], nl, nh, r);
+            for (int k = 0; k < 3; k++)
+                if (!(fmin(nh[k], hi[k]) >= fmax(nl[k], lo[k]))) return false;
+            return true;
+        },
+        [&](u32 leaf) {
+            for (u32 rr = t.reduc[leaf]; rr < t.reduc[leaf + 1]; rr++) {
+                bool in = true;
+                if (mode == 1) {
+                    f64 p[3] = {sx[rr], sy[rr], sz[rr]};
+                    for (int k = 0; k < 3; k++)
+                        if (!(fmin(p[k], hi[k]) >= fmax(p[k], lo[k]))) in = false;
+                }
+                if (in) {
+                    if (FILL) out[w++] = sort_index[rr];
+                    c++;
+                }
+            }
+        });
+    if (!ok) atomicOr(flags, kFlagStackOverflow);
+    if (!FILL) counts[q] = c;
+}
+
+TreeView view(const Ctx &c) {
+    return TreeView{c.lchild.as<u32>(), c.rchild.as<u32>(), c.lflag.as<u8>(), c.rflag.as<u8>(),
+                    c.boxes.as<NodeBox>(), c.reduc.as<u32>(), c.leaf_count};
+}
+
+} // namespace
+
+cudaError_t build_rows(Ctx &c, u32 n_local) {
+    cudaStream_t s = c.stream;
+    cudaError_t e;
+    u32 N = c.n_obj;
+    if ((e = c.row_flags.ensure(N, s)) != cudaSuccess) return e;
+    if ((e = c.row_offsets.ensure(sizeof(u32) * (size_t) N, s)) != cudaSuccess) return e;
+    if ((e = c.row_rank.ensure(sizeof(u32) * (size_t) n_local, s)) != cudaSuccess) return e;
+    if ((e = c.row_local.ensure(sizeof(u32) * (size_t) n_local, s)) != cudaSuccess) return e;
+    { k_row_flags<<<div_up(N, 256), 256, 0, s>>>(c.sort_index.as<u32>(), N, n_local,
+                                               c.row_flags.as<u8>()); GBSPH_COUNTED; }
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    if ((e = scan_exclusive_flags(c.row_flags.as<u8>(), c.row_offsets.as<u32>(), N, &dsc->total2,
+                                  c.scan_scratch, s)) != cudaSuccess)
+        return e;
+    { k_rows<<<div_up(N, 256), 256, 0, s>>>(c.sort_index.as<u32>(), c.row_flags.as<u8>(),
+                                          c.row_offsets.as<u32>(), N, c.row_rank.as<u32>(),
+                                          c.row_local.as<u32>()); GBSPH_COUNTED; }
+    c.n_local = n_local;
+    return cudaGetLastError();
+}
+
+cudaError_t neigh_cache_build(Ctx &c, f64 h_tol) {
+    cudaStream_t s = c.stream;
+    cudaError_t e;
+    u32 L = c.leaf_count, n = c.n_local;
+    TreeView t = view(c);
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    if ((e = c.leaf_cnt.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+    if ((e = c.leaf_off.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+    {
+        ProfScope ps(c, kProfStage1, L);
+        { k_leaf_count<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_cnt.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
+        if ((e = scan_exclusive_u32(c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), L, &dsc->total,
+                                    c.scan_scratch, s)) != cudaSuccess)
+            return e;
+    }
+    if ((e = c.owner.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
+    if (n) {
+        ProfScope ps(c, kProfOwner, n);
+        { k_owner<<<div_up(n, 128), 128, 0, s>>>(t, c.row_rank.as<u32>(), n, c.sx.as<f64>(),
+                                               c.sy.as<f64>(), c.sz.as<f64>(), c.owner.as<u32>(),
+                                               &dsc->flags); GBSPH_COUNTED; }
+    }
+    if ((e = sync_scalars(c)) != cudaSuccess) return e;
+    c.leaf_csr_total = c.h_scalars->total;
+    if (c.h_scalars->flags & (kFlagStackOverflow | kFlagOwnerMissing)) {
+        c.err = "neighbour cache: tree traversal failed (stack overflow or particle outside every leaf box)";
+        return cudaErrorUnknown;
+    }
+    if ((e = c.leaf_ent.ensure(sizeof(u32) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
+    {
+        ProfScope ps(c, kProfStage1, 0);
+        { k_leaf_fill<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_off.as<u32>(), c.leaf_ent.as<u32>()); GBSPH_COUNTED; }
+    }
+
+    if ((e = c.csr_cnt.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
+    if ((e = c.csr_off.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
+    if (n) {
+        ProfScope ps(c, kProfCacheCount, n);
+        { k_part_cache<false><<<div_up(n, 256), 256, 0, s>>>(
+            c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
+            c.leaf_ent.as<u32>(), c.reduc.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
+            c.sh.as<f64>(), h_tol, c.csr_cnt.as<u32>(), nullptr, nullptr); GBSPH_COUNTED; }
+    }
+    if ((e = scan_exclusive_u32(c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), n, &dsc->total,
+                                c.scan_scratch, s)) != cudaSuccess)
+        return e;
+    if ((e = sync_scalars(c)) != cudaSuccess) return e;
+    c.csr_total = c.h_scalars->total;
+    if ((e = c.csr_ent.ensure(sizeof(u32) * (c.csr_total + 1), s)) != cudaSuccess) return e;
+    if (n) {
+        ProfScope ps(c, kProfCacheFill, c.csr_total);
+        { k_part_cache<true><<<div_up(n, 256), 256, 0, s>>>(
+            c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
+            c.leaf_ent.as<u32>(), c.reduc.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
+            c.sh.as<f64>(), h_tol, nullptr, c.csr_off.as<u32>(), c.csr_ent.as<u32>()); GBSPH_COUNTED; }
+    }
+    c.cache_valid = true;
+    return cudaGetLastError();
+}
+
+cudaError_t tree_query(Ctx &c, const f64 *qx, const f64 *qy, const f64 *qz, u32 nq, int mode,
+                       f64 s, u32 *counts, u32 *offsets, u32 *out, bool fill) {
+    TreeView t = view(c);
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    if (fill)
+        { k_query<true><<<div_up(nq, 128), 128, 0, c.stream>>>(
+            t, qx, qy, qz, nq, mode, s, c.sort_index.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(),
+            c.sz.as<f64>(), nullptr, offsets, out, &dsc->flags); GBSPH_COUNTED; }
+    else
+        { k_query<false><<<div_up(nq, 128), 128, 0, c.stream>>>(
+            t, qx, qy, qz, nq, mode, s, c.sort_index.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(),
+            c.sz.as<f64>(), counts, nullptr, nullptr, &dsc->flags); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+} // namespace gbsph

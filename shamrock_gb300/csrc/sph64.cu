@@ -1,0 +1,454 @@
+// FP64 SPH pair kernels and integrator.  This translation unit is compiled with
+// fused multiply-add disabled so that every expression rounds exactly as the cited
+// reference line (and the oracle) evaluates it; the FP64 path is bit-identical to
+// the oracle for the same neighbour order.
+//
+//   h-rho Newton step  shammodels/sph/src/modules/IterateSmoothingLengthDensity.cpp:52-119
+//                      shammodels/sph/include/shammodels/sph/math/density.hpp:22-41
+//   Omega              shammodels/sph/src/modules/ComputeOmega.cpp:36-73
+//   EOS (adiabatic)    shammodels/sph/src/modules/ComputeEos.cpp:162-172,219-236
+//   derivatives        shammodels/sph/src/modules/UpdateDerivs.cpp:176-271,
+//                      shammodels/sph/include/shammodels/sph/math/forces.hpp:24-226, q_ab.hpp:36-39
+//   v_sig              shammodels/sph/src/Solver.cpp:2716-2788
+//   CFL                ComputeCFLCourant.hpp:45-60, ComputeCFLForce.hpp:50-62
+//   corrector          shamrock/src/math/integrators.cpp:88-120, Solver.cpp:2506-2616
+//   predictor + wrap   Solver.cpp:390-524, ForwardEuler.hpp:62-84, integrators.cpp:207-237
+
+#include "gbsph_ctx.cuh"
+#include "sph_kernels.cuh"
+
+namespace gbsph {
+
+namespace {
+
+// ---------------------------------------------------------------- M4 (FP64)
+__device__ __forceinline__ f64 m4_f(f64 q) {
+    f64 t1 = 2 - q;
+    f64 t2 = 1 - q;
+    t1     = t1 * t1 * t1;
+    t2     = t2 * t2 * t2;
+    const f64 div1_4 = (1. / 4.);
+    t1 *= div1_4;
+    t2 *= -1;
+    if (q < 1) return t1 + t2;
+    else if (q < 2) return t1;
+    return 0;
+}
+__device__ __forceinline__ f64 m4_df(f64 q) {
+    const f64 div9_4 = (9. / 4.);
+    const f64 div3_4 = (3. / 4.);
+    if (q < 1) return -3 * q + div9_4 * q * q;
+    else if (q < 2) return -3 + 3 * q - div3_4 * q * q;
+    return 0;
+}
+__device__ __forceinline__ f64 W_3d(f64 r, f64 h) { return kNorm3d * m4_f(r / h) / (h * h * h); }
+__device__ __forceinline__ f64 dW_3d(f64 r, f64 h) {
+    return kNorm3d * m4_df(r / h) / (h * h * h * h);
+}
+__device__ __forceinline__ f64 dhW_3d(f64 r, f64 h) {
+    return -(kNorm3d) * (3 * m4_f(r / h) + (r / h) * m4_df(r / h)) / (h * h * h * h);
+}
+__device__ __forceinline__ f64 rho_h(f64 m, f64 h) {
+    return m * (kHfact / h) * (kHfact / h) * (kHfact / h);
+}
+__device__ __forceinline__ f64 inv_sat_positive(f64 v) { return (v >= 1e-9) ? 1. / v : 0.; }
+__device__ __forceinline__ f64 inv_sat_zero(f64 v) { return (v != 0 && v == v) ? 1. / v : 0.; }
+
+// ---------------------------------------------------------------- density sums
+__device__ __forceinline__ void density_sums(const RowSpace &rs, u32 a, u32 k0, u32 k1, f64 h_a,
+                                             f64 pmass, f64 &rho_sum, f64 &sumdWdh) {
+    f64 xa = rs.x[a], ya = rs.y[a], za = rs.z[a];
+    f64 dint = h_a * h_a * kRkern * kRkern;
+    rho_sum  = 0;
+    sumdWdh  = 0;
+    for (u32 k = k0; k < k1; k++) {
+        u32 b    = rs.ent[k];
+        f64 dx   = xa - rs.x[b], dy = ya - rs.y[b], dz = za - rs.z[b];
+        f64 rab2 = dx * dx + dy * dy + dz * dz;
+        if (rab2 > dint) continue;
+        f64 rab = sqrt(rab2);
+        rho_sum += pmass * W_3d(rab, h_a);
+        sumdWdh += pmass * dhW_3d(rab, h_a);
+    }
+}
+
+// ITERS Newton iterations per row (the reference's global loop is equivalent per
+// particle: a particle's update reads only its own h, so it iterates until its own
+// eps <= 1e-6, becomes -1, or the iteration cap is reached).
+__global__ void __launch_bounds__(256) k_h_iterate(RowSpace rs, const f64 *__restrict__ h_old,
+                                                   f64 *__restrict__ h_new, f64 *__restrict__ eps,
+                                                   f64 pmass, f64 h_evol_max, f64 h_evol_iter_max,
+                                                   u32 iters, Scalars *sc) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    u64 emax = 0, emin = ~0ull;
+    u32 used = 0;
+    if (t < rs.n) {
+        u32 a  = rs.row_rank ? rs.row_rank[t] : t;
+        u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+        const f64 h_max_tot_max_evol = h_evol_max;
+        const f64 h_max_evol_p       = h_evol_iter_max;
+        const f64 h_max_evol_m       = 1 / h_evol_iter_max;
+        f64 ha_0 = h_old[t];
+        f64 h_a  = h_new[t];
+        f64 e    = eps[t];
+        for (u32 it = 0; it < iters; it++) {
+            if (!(e > 1e-6)) break;
+            used++;
+            f64 rho_sum, sumdWdh;
+            density_sums(rs, a, k0, k1, h_a, pmass, rho_sum, sumdWdh);
+            f64 rho_ha  = rho_h(pmass, h_a);
+            f64 f_iter  = rho_sum - rho_ha;
+            f64 df_iter = sumdWdh + 3 * rho_ha / h_a;
+            f64 new_h   = h_a - f_iter / df_iter;
+            if (new_h < h_a * h_max_evol_m) new_h = h_max_evol_m * h_a;
+            if (new_h > h_a * h_max_evol_p) new_h = h_max_evol_p * h_a;
+            if (new_h < ha_0 * h_max_tot_max_evol) {
+                e   = fabs(new_h - h_a) / ha_0;
+                h_a = new_h;
+            } else {
+                h_a = ha_0 * h_max_tot_max_evol;
+                e   = -1;
+            }
+        }
+        h_new[t] = h_a;
+        eps[t]   = e;
+        emax     = f64_to_ordered(e);
+        emin     = emax;
+    }
+    emax = block_reduce(emax, OpMaxU64{}, 0ull);
+    emin = block_reduce(emin, OpMinU64{}, ~0ull);
+    u32 um = block_reduce((u64) used, OpMaxU64{}, 0ull);
+    if (threadIdx.x == 0) {
+        atomicMax((unsigned long long *) &sc->eps_max, (unsigned long long) emax);
+        atomicMin((unsigned long long *) &sc->eps_min, (unsigned long long) emin);
+        atomicMax(&sc->iters_max, um);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_omega(RowSpace rs, const f64 *__restrict__ h_row,
+                                               f64 pmass, f64 *__restrict__ omega_out,
+                                               const u32 *__restrict__ out_index) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    u32 a  = rs.row_rank ? rs.row_rank[t] : t;
+    u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    f64 h_a = h_row[t];
+    f64 rho_sum, part_omega_sum;
+    density_sums(rs, a, k0, k1, h_a, pmass, rho_sum, part_omega_sum);
+    f64 rho_ha  = rho_h(pmass, h_a);
+    f64 omega_a = 1 + (h_a / (3 * rho_ha)) * part_omega_sum;
+    omega_out[out_index ? out_index[t] : t] = omega_a;
+}
+
+// gather h, u, v, omega of locals and ghosts into rank order + adiabatic EOS
+__global__ void k_gather_eos(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
+                             const u32 *__restrict__ ghost_src, const f64 *__restrict__ h,
+                             const f64 *__restrict__ u, const f64 *__restrict__ vx,
+                             const f64 *__restrict__ vy, const f64 *__restrict__ vz, u32 vs,
+                             const f64 *__restrict__ omega, f64 pmass, f64 gamma,
+                             f64 *__restrict__ sh, f64 *__restrict__ su, f64 *__restrict__ svx,
+                             f64 *__restrict__ svy, f64 *__restrict__ svz, f64 *__restrict__ som,
+                             f64 *__restrict__ sP, f64 *__restrict__ scs) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    u32 id  = sort_index[r];
+    u32 src = id < n_local ? id : ghost_src[id - n_local];
+    f64 hh = h[src], uu = u[src];
+    sh[r]  = hh;
+    su[r]  = uu;
+    svx[r] = vx[(size_t) src * vs];
+    svy[r] = vy[(size_t) src * vs];
+    svz[r] = vz[(size_t) src * vs];
+    som[r] = omega[src];
+    f64 rho = rho_h(pmass, hh);
+    f64 P   = (gamma - 1) * rho * uu;
+    sP[r]   = P;
+    scs[r]  = sqrt(gamma * P / rho);
+}
+
+__global__ void k_eos(u32 n, const f64 *__restrict__ h, const f64 *__restrict__ u, f64 pmass,
+                      f64 gamma, f64 *__restrict__ P, f64 *__restrict__ cs) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f64 rho = rho_h(pmass, h[i]);
+    f64 Pa  = (gamma - 1) * rho * u[i];
+    P[i]    = Pa;
+    cs[i]   = sqrt(gamma * Pa / rho);
+}
+
+// ---------------------------------------------------------------- derivatives
+struct DerivParams {
+    f64 pmass, alpha_u, alpha_AV, beta_AV;
+    f64 hdt;             // dt / 2 for the corrector
+    f64 C_cour, C_force; // CFL factors (already x cfl multiplier)
+};
+
+template<bool VSIG>
+__device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace &hs, u32 a, u32 k0,
+                                           u32 k1, const DerivParams &p, f64 &fx, f64 &fy, f64 &fz,
+                                           f64 &tdu, f64 &vsig_max) {
+    const f64 Rker2 = kRkern * kRkern;
+    f64 h_a = hs.h[a];
+    f64 xa = rs.x[a], ya = rs.y[a], za = rs.z[a];
+    f64 vxa = hs.vx[a], vya = hs.vy[a], vza = hs.vz[a];
+    f64 P_a = hs.P[a], omega_a = hs.omega[a];
+    const f64 u_a         = hs.u[a];
+    f64 rho_a             = rho_h(p.pmass, h_a);
+    f64 rho_a_sq          = rho_a * rho_a;
+    f64 rho_a_inv         = 1. / rho_a;
+    f64 omega_a_rho_a_inv = 1 / (omega_a * rho_a);
+    f64 cs_a              = hs.cs[a];
+    fx = fy = fz = tdu = 0;
+    vsig_max           = 0;
+    for (u32 k = k0; k < k1; k++) {
+        u32 b    = rs.ent[k];
+        f64 dx   = xa - rs.x[b], dy = ya - rs.y[b], dz = za - rs.z[b];
+        f64 rab2 = dx * dx + dy * dy + dz * dz;
+        f64 h_b  = hs.h[b];
+        if (rab2 > h_a * h_a * Rker2 && rab2 > h_b * h_b * Rker2) continue;
+        f64 rab       = sqrt(rab2);
+        const f64 u_b = hs.u[b];
+        f64 rho_b   = rho_h(p.pmass, h_b);
+        f64 P_b     = hs.P[b];
+        f64 omega_b = hs.omega[b];
+        f64 cs_b    = hs.cs[b];
+        f64 Fab_a   = dW_3d(rab, h_a);
+        f64 Fab_b   = dW_3d(rab, h_b);
+        f64 vx = vxa - hs.vx[b], vy = vya - hs.vy[b], vz = vza - hs.vz[b];
+        f64 inv = inv_sat_positive(rab);
+        f64 rx = dx * inv, ry = dy * inv, rz = dz * inv;
+        f64 v_ab_r_ab     = vx * rx + vy * ry + vz * rz;
+        f64 abs_v_ab_r_ab = fabs(v_ab_r_ab);
+        f64 vsig_a  = p.alpha_AV * cs_a + p.beta_AV * abs_v_ab_r_ab;
+        f64 vsig_b  = p.alpha_AV * cs_b + p.beta_AV * abs_v_ab_r_ab;
+        f64 rho_avg = (rho_a + rho_b) * 0.5;
+        f64 abs_dp  = fabs(P_a - P_b);
+        f64 vsig_u  = sqrt(abs_dp / rho_avg);
+        f64 qa_ab   = fmax(-f64(0.5) * rho_a * vsig_a * v_ab_r_ab, f64(0));
+        f64 qb_ab   = fmax(-f64(0.5) * rho_b * vsig_b * v_ab_r_ab, f64(0));
+        f64 AV_P_a  = P_a + qa_ab;
+        f64 AV_P_b  = P_b + qb_ab;
+        f64 sub_fact_a = rho_a_sq * omega_a;
+        f64 sub_fact_b = (rho_b * rho_b) * omega_b;
+        f64 ca = AV_P_a * inv_sat_zero(sub_fact_a);
+        f64 cb = AV_P_b * inv_sat_zero(sub_fact_b);
+        f64 nax = rx * Fab_a, nay = ry * Fab_a, naz = rz * Fab_a;
+        f64 nbx = rx * Fab_b, nby = ry * Fab_b, nbz = rz * Fab_b;
+        f64 mb = -p.pmass;
+        fx += mb * (ca * nax + cb * nbx);
+        fy += mb * (ca * nay + cb * nby);
+        fz += mb * (ca * naz + cb * nbz);
+        f64 dotvg = vx * nax + vy * nay + vz * naz;
+        tdu += AV_P_a * (omega_a_rho_a_inv * rho_a_inv) * p.pmass * dotvg;
+        f64 Fa = Fab_a * omega_a_rho_a_inv;
+        f64 Fb = Fab_b / (rho_b * omega_b);
+        tdu += p.pmass * p.alpha_u * vsig_u * (u_a - u_b) * f64(0.5) * (Fa + Fb);
+        if (VSIG) {
+            // separate v_sig kernel of the reference: r_hat = dr / r, zero below 1e-9,
+            // alpha = 1, beta = 2 fixed
+            f64 ux = dx / rab, uy = dy / rab, uz = dz / rab;
+            if (rab < 1e-9) ux = uy = uz = 0;
+            f64 vr = vx * ux + vy * uy + vz * uz;
+            f64 vs = 1.0 * cs_a + 2.0 * fabs(vr);
+            vsig_max = fmax(vsig_max, vs);
+        }
+    }
+}
+
+// module form: reference CSR, outputs a, du (and vsig) by row
+__global__ void __launch_bounds__(128) k_derivs(RowSpace rs, HydroSpace hs, DerivParams p,
+                                                f64 *__restrict__ ax, f64 *__restrict__ ay,
+                                                f64 *__restrict__ az, f64 *__restrict__ du,
+                                                f64 *__restrict__ vsig) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    u32 a  = rs.row_rank ? rs.row_rank[t] : t;
+    u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    f64 fx, fy, fz, tdu, vm;
+    if (vsig) derivs_row<true>(rs, hs, a, k0, k1, p, fx, fy, fz, tdu, vm);
+    else derivs_row<false>(rs, hs, a, k0, k1, p, fx, fy, fz, tdu, vm);
+    ax[t] = fx;
+    ay[t] = fy;
+    az[t] = fz;
+    du[t] = tdu;
+    if (vsig) vsig[t] = vm;
+}
+
+// pipeline form: derivatives + v_sig + leapfrog corrector + CFL, outputs to the
+// caller's local arrays.  Neighbour velocities come from the rank-ordered copy
+// taken before the corrector, so correcting the caller's v here is race-free.
+__global__ void __launch_bounds__(128) k_derivs_step(RowSpace rs, HydroSpace hs, DerivParams p,
+                                                     LocalFields lf, Scalars *sc) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    u64 ev2 = 0, dtm = ~0ull;
+    f64 v2  = 0;
+    if (t < rs.n) {
+        u32 a  = rs.row_rank[t];
+        u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+        f64 fx, fy, fz, tdu, vm;
+        derivs_row<true>(rs, hs, a, k0, k1, p, fx, fy, fz, tdu, vm);
+        u32 i  = rs.row_local[t];
+        size_t iv = (size_t) i * lf.vs;
+        f64 ox = lf.ax[iv], oy = lf.ay[iv], oz = lf.az[iv], odu = lf.du[i];
+        lf.ax[iv] = fx;
+        lf.ay[iv] = fy;
+        lf.az[iv] = fz;
+        lf.du[i]  = tdu;
+        // corrector (integrators.cpp:88-120): incr = hdt * (new - old)
+        f64 ix = p.hdt * (fx - ox), iy = p.hdt * (fy - oy), iz = p.hdt * (fz - oz);
+        f64 nvx = lf.vx[iv] + ix, nvy = lf.vy[iv] + iy, nvz = lf.vz[iv] + iz;
+        lf.vx[iv] = nvx;
+        lf.vy[iv] = nvy;
+        lf.vz[iv] = nvz;
+        f64 iu    = p.hdt * (tdu - odu);
+        lf.u[i]   = lf.u[i] + iu;
+        ev2       = f64_to_ordered(ix * ix + iy * iy + iz * iz);
+        v2        = nvx * nvx + nvy * nvy + nvz * nvz;
+        // CFL with the new acceleration
+        f64 h_a  = hs.h[a];
+        f64 dt   = __longlong_as_double(0x7ff0000000000000ll);
+        f64 dt_c = p.C_cour * h_a / vm;
+        dt       = fmin(dt, dt_c);
+        f64 abs_a = sqrt(fx * fx + fy * fy + fz * fz);
+        f64 dt_f  = p.C_force * sqrt(h_a / abs_a);
+        dt        = fmin(dt, dt_f);
+        dtm       = f64_to_ordered(dt);
+    }
+    ev2 = block_reduce(ev2, OpMaxU64{}, 0ull);
+    dtm = block_reduce(dtm, OpMinU64{}, ~0ull);
+    v2  = block_reduce(v2, OpAddF64{}, 0.0);
+    if (threadIdx.x == 0) {
+        atomicMax((unsigned long long *) &sc->epsv2_max, (unsigned long long) ev2);
+        atomicMin((unsigned long long *) &sc->dt_min, (unsigned long long) dtm);
+        atomicAdd(&sc->sum_v2, v2);
+    }
+}
+
+// leapfrog predictor (half kick, drift, half kick) + periodic wrap, one pass
+__global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f64 b1, f64 b2,
+                          f64 e0, f64 e1, f64 e2) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t iv   = (size_t) i * lf.vs;
+    f64 dt_half = dt / 2;
+    f64 ax = lf.ax[iv], ay = lf.ay[iv], az = lf.az[iv], dd = lf.du[i];
+    f64 vx = lf.vx[iv], vy = lf.vy[iv], vz = lf.vz[iv], u = lf.u[i];
+    vx = vx + dt_half * ax;
+    vy = vy + dt_half * ay;
+    vz = vz + dt_half * az;
+    u  = u + dt_half * dd;
+    f64 x = lf.x[iv] + dt * vx, y = lf.y[iv] + dt * vy, z = lf.z[iv] + dt * vz;
+    vx = vx + dt_half * ax;
+    vy = vy + dt_half * ay;
+    vz = vz + dt_half * az;
+    u  = u + dt_half * dd;
+    if (periodic) {
+        f64 bmin[3] = {b0, b1, b2}, bmax[3] = {e0, e1, e2};
+        f64 p[3]    = {x, y, z};
+        for (int c = 0; c < 3; c++) {
+            f64 delt = bmax[c] - bmin[c];
+            f64 r    = p[c] - bmin[c];
+            r        = fmod(r, delt);
+            r += delt;
+            r = fmod(r, delt);
+            r += bmin[c];
+            p[c] = r;
+        }
+        x = p[0];
+        y = p[1];
+        z = p[2];
+    }
+    lf.x[iv]  = x;
+    lf.y[iv]  = y;
+    lf.z[iv]  = z;
+    lf.vx[iv] = vx;
+    lf.vy[iv] = vy;
+    lf.vz[iv] = vz;
+    lf.u[i]   = u;
+}
+
+__global__ void k_scatter_rows(u32 n, const u32 *__restrict__ row_local, const f64 *__restrict__ src,
+                               f64 *__restrict__ dst) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    dst[row_local[t]] = src[t];
+}
+
+__global__ void k_gather_rows(u32 n, const u32 *__restrict__ row_rank, const f64 *__restrict__ src,
+                              f64 *__restrict__ dst, f64 *__restrict__ dst2) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    f64 v  = src[row_rank[t]];
+    dst[t] = v;
+    if (dst2) dst2[t] = v;
+}
+
+__global__ void k_fill(u32 n, f64 *__restrict__ dst, f64 v) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = v;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------- host wrappers
+cudaError_t h_iterate64(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
+                        f64 pmass, f64 hev, f64 hevi, u32 iters) {
+    ProfScope ps(c, kProfHIter, rs.n);
+    { k_h_iterate<<<div_up(rs.n, 256), 256, 0, c.stream>>>(rs, h_old, h_new, eps, pmass, hev, hevi,
+                                                         iters, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t omega64(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *out,
+                    const u32 *out_index) {
+    ProfScope ps(c, kProfOmega, rs.n);
+    { k_omega<<<div_up(rs.n, 256), 256, 0, c.stream>>>(rs, h_row, pmass, out, out_index); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t eos64(Ctx &c, u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamma, f64 *P, f64 *cs) {
+    { k_eos<<<div_up(n, 256), 256, 0, c.stream>>>(n, h, u, pmass, gamma, P, cs); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t gather_eos64(Ctx &c, u32 N, u32 n_local, const LocalFields &lf, const f64 *omega_local,
+                         f64 pmass, f64 gamma) {
+    ProfScope ps(c, kProfGatherEos, N);
+    { k_gather_eos<<<div_up(N, 256), 256, 0, c.stream>>>(
+        c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf.h, lf.u, lf.vx, lf.vy, lf.vz,
+        lf.vs, omega_local, pmass, gamma, c.sh2.as<f64>(), c.su.as<f64>(), c.svx.as<f64>(),
+        c.svy.as<f64>(), c.svz.as<f64>(), c.som.as<f64>(), c.sP.as<f64>(), c.scs.as<f64>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t derivs64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
+                     f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az, f64 *du, f64 *vsig) {
+    DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, 0, 0, 0};
+    { k_derivs<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, ax, ay, az, du, vsig); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
+                          f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
+                          const LocalFields &lf) {
+    DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, hdt, C_cour, C_force};
+    ProfScope ps(c, kProfDerivs, rs.n);
+    { k_derivs_step<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, lf, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic, const f64 *bmin,
+                      const f64 *bmax) {
+    ProfScope ps(c, kProfPredict, n);
+    { k_predict<<<div_up(n, 256), 256, 0, c.stream>>>(lf, n, dt, periodic, bmin[0], bmin[1], bmin[2],
+                                                   bmax[0], bmax[1], bmax[2]); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t scatter_rows(Ctx &c, u32 n, const f64 *src, f64 *dst) {
+    { k_scatter_rows<<<div_up(n, 256), 256, 0, c.stream>>>(n, c.row_local.as<u32>(), src, dst); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t gather_rows(Ctx &c, u32 n, const f64 *src_rank, f64 *dst, f64 *dst2) {
+    { k_gather_rows<<<div_up(n, 256), 256, 0, c.stream>>>(n, c.row_rank.as<u32>(), src_rank, dst, dst2); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t fill64(Ctx &c, u32 n, f64 *dst, f64 v) {
+    { k_fill<<<div_up(n, 256), 256, 0, c.stream>>>(n, dst, v); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+} // namespace gbsph

@@ -1,0 +1,58 @@
+// Argument bundles of the SPH pair kernels and the host wrappers that launch them.
+#pragma once
+
+#include "gbsph_ctx.cuh"
+
+namespace gbsph {
+
+// A set of CSR rows and the index space their entries live in.
+//  - module form (reference layout): row t is local particle t, entries are merged
+//    ids, positions are indexed by merged id; row_rank == row_local == nullptr.
+//  - pipeline form: row t is the t-th local particle in Morton order,
+//    row_rank[t] its rank, row_local[t] its local id; entries are ranks and
+//    positions are the rank-ordered copies.
+struct RowSpace {
+    u32 n;
+    const u32 *row_rank;
+    const u32 *row_local;
+    const u32 *cnt;
+    const u32 *off;
+    const u32 *ent;
+    const f64 *x, *y, *z;
+};
+
+// Hydro fields in the same index space as the CSR entries.
+struct HydroSpace {
+    const f64 *h, *u, *vx, *vy, *vz, *omega, *P, *cs;
+};
+
+// The caller's per-particle arrays (local ids).  Vector components are separate
+// pointers sharing the element stride vs (1 for SoA, 3 or 4 for AoS f64_3).
+struct LocalFields {
+    f64 *x, *y, *z;
+    f64 *vx, *vy, *vz;
+    f64 *ax, *ay, *az;
+    u32 vs;
+    f64 *h, *u, *du;
+};
+
+// sph64.cu
+cudaError_t h_iterate64(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
+                        f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters);
+cudaError_t omega64(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *out,
+                    const u32 *out_index);
+cudaError_t eos64(Ctx &c, u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamma, f64 *P, f64 *cs);
+cudaError_t gather_eos64(Ctx &c, u32 N, u32 n_local, const LocalFields &lf, const f64 *omega_local,
+                         f64 pmass, f64 gamma);
+cudaError_t derivs64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
+                     f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az, f64 *du, f64 *vsig);
+cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
+                          f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
+                          const LocalFields &lf);
+cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic, const f64 *bmin,
+                      const f64 *bmax);
+cudaError_t scatter_rows(Ctx &c, u32 n, const f64 *src, f64 *dst);
+cudaError_t gather_rows(Ctx &c, u32 n, const f64 *src_rank, f64 *dst, f64 *dst2);
+cudaError_t fill64(Ctx &c, u32 n, f64 *dst, f64 v);
+
+} // namespace gbsph

@@ -1,0 +1,364 @@
+// Mixed-precision SPH pair kernels: the per-pair arithmetic of the h-rho Newton
+// sums, Omega and the constant-AV derivatives runs in FP32 on hi/lo-split positions
+// and velocities, with Kahan-compensated FP32 neighbour sums.  FP64 is kept for the
+// absolute positions, the Newton update and its convergence test (eps_h), the
+// leapfrog corrector and CFL, and the global totals.  Same physics and neighbour
+// set as the FP64 kernels (sph64.cu); see those for the reference citations.
+
+#include "sph_mixed.cuh"
+
+namespace gbsph {
+
+namespace {
+
+constexpr float kNorm3dF = 0.318309886183790671538f; // 1/pi
+
+__device__ __forceinline__ float m4_f32(float q) {
+    float t1 = 2.f - q, t2 = 1.f - q;
+    t1 = t1 * t1 * t1 * 0.25f;
+    t2 = -(t2 * t2 * t2);
+    return q < 1.f ? t1 + t2 : (q < 2.f ? t1 : 0.f);
+}
+__device__ __forceinline__ float m4_df32(float q) {
+    return q < 1.f ? (-3.f * q + 2.25f * q * q) : (q < 2.f ? (-3.f + 3.f * q - 0.75f * q * q) : 0.f);
+}
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c       = (t - s) - y;
+    s       = t;
+}
+__device__ __forceinline__ float hi32(f64 v) { return __double2float_rn(v); }
+__device__ __forceinline__ float lo32(f64 v) { return __double2float_rn(v - (f64) __double2float_rn(v)); }
+
+__device__ __forceinline__ f64 rho_h64(f64 m, f64 h) {
+    return m * (kHfact / h) * (kHfact / h) * (kHfact / h);
+}
+
+__global__ void k_stage_pos(u32 N, const f64 *__restrict__ sx, const f64 *__restrict__ sy,
+                            const f64 *__restrict__ sz, const f64 *__restrict__ sh,
+                            float4 *__restrict__ A, float4 *__restrict__ B) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    f64 x = sx[r], y = sy[r], z = sz[r];
+    A[r] = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / sh[r]));
+    B[r] = make_float4(lo32(x), lo32(y), lo32(z), 0.f);
+}
+
+// hydro staging from FP64 fields in the entry index space
+__global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__restrict__ y,
+                              const f64 *__restrict__ z, HydroSpace hs, f64 pmass,
+                              float4 *__restrict__ A, float4 *__restrict__ B,
+                              float4 *__restrict__ C, float4 *__restrict__ D,
+                              float4 *__restrict__ E) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    f64 h = hs.h[r], om = hs.omega[r], P = hs.P[r];
+    f64 rho = rho_h64(pmass, h);
+    float hinv = __double2float_rn(1.0 / h);
+    if (x) {
+        A[r] = make_float4(hi32(x[r]), hi32(y[r]), hi32(z[r]), hinv);
+        B[r] = make_float4(lo32(x[r]), lo32(y[r]), lo32(z[r]), __double2float_rn(hs.cs[r]));
+    } else {
+        ((float *) &A[r])[3] = hinv;
+        ((float *) &B[r])[3] = __double2float_rn(hs.cs[r]);
+    }
+    f64 vx = hs.vx[r], vy = hs.vy[r], vz = hs.vz[r];
+    C[r] = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(hs.u[r]));
+    D[r] = make_float4(lo32(vx), lo32(vy), lo32(vz), __double2float_rn(rho));
+    f64 sub = rho * rho * om;
+    f64 c1  = (sub != 0 && sub == sub) ? 1. / sub : 0.;
+    E[r]    = make_float4(hi32(P), lo32(P), __double2float_rn(c1), __double2float_rn(1. / (rho * om)));
+}
+
+// sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a
+__device__ __forceinline__ void density_sums_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
+                                                 u32 k0, u32 k1, float hinv, float &sf, float &sg) {
+    float4 Aa = __ldg(&ms.A[a]), Ba = __ldg(&ms.B[a]);
+    float cf = 0.f, cg = 0.f;
+    sf = 0.f;
+    sg = 0.f;
+    float hinv2 = hinv * hinv;
+    for (u32 k = k0; k < k1; k++) {
+        u32 b     = __ldg(&rs.ent[k]);
+        float4 Ab = __ldg(&ms.A[b]), Bb = __ldg(&ms.B[b]);
+        float dx = (Aa.x - Ab.x) + (Ba.x - Bb.x);
+        float dy = (Aa.y - Ab.y) + (Ba.y - Bb.y);
+        float dz = (Aa.z - Ab.z) + (Ba.z - Bb.z);
+        float q2 = (dx * dx + dy * dy + dz * dz) * hinv2;
+        if (q2 > 4.f) continue;
+        float q  = sqrtf(q2);
+        float f  = m4_f32(q);
+        float df = m4_df32(q);
+        kahan_add(sf, cf, f);
+        kahan_add(sg, cg, 3.f * f + q * df);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_h_iterate_mixed(RowSpace rs, MixedSpace ms,
+                                                         const f64 *__restrict__ h_old,
+                                                         f64 *__restrict__ h_new,
+                                                         f64 *__restrict__ eps, f64 pmass,
+                                                         f64 h_evol_max, f64 h_evol_iter_max,
+                                                         u32 iters, Scalars *sc) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    u64 emax = 0, emin = ~0ull;
+    u32 used = 0;
+    if (t < rs.n) {
+        u32 a  = rs.row_rank ? rs.row_rank[t] : t;
+        u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+        const f64 h_max_evol_m = 1 / h_evol_iter_max;
+        f64 ha_0 = h_old[t], h_a = h_new[t], e = eps[t];
+        for (u32 it = 0; it < iters; it++) {
+            if (!(e > 1e-6)) break;
+            used++;
+            float sf, sg;
+            density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(1.0 / h_a), sf, sg);
+            f64 h3      = h_a * h_a * h_a;
+            f64 rho_sum = pmass * kNorm3d * (f64) sf / h3;
+            f64 sumdWdh = -pmass * kNorm3d * (f64) sg / (h3 * h_a);
+            f64 rho_ha  = rho_h64(pmass, h_a);
+            f64 new_h   = h_a - (rho_sum - rho_ha) / (sumdWdh + 3 * rho_ha / h_a);
+            if (new_h < h_a * h_max_evol_m) new_h = h_max_evol_m * h_a;
+            if (new_h > h_a * h_evol_iter_max) new_h = h_evol_iter_max * h_a;
+            if (new_h < ha_0 * h_evol_max) {
+                e   = fabs(new_h - h_a) / ha_0;
+                h_a = new_h;
+            } else {
+                h_a = ha_0 * h_evol_max;
+                e   = -1;
+            }
+        }
+        h_new[t] = h_a;
+        eps[t]   = e;
+        emax     = f64_to_ordered(e);
+        emin     = emax;
+    }
+    emax   = block_reduce(emax, OpMaxU64{}, 0ull);
+    emin   = block_reduce(emin, OpMinU64{}, ~0ull);
+    u64 um = block_reduce((u64) used, OpMaxU64{}, 0ull);
+    if (threadIdx.x == 0) {
+        atomicMax((unsigned long long *) &sc->eps_max, (unsigned long long) emax);
+        atomicMin((unsigned long long *) &sc->eps_min, (unsigned long long) emin);
+        atomicMax(&sc->iters_max, (u32) um);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_omega_mixed(RowSpace rs, MixedSpace ms,
+                                                     const f64 *__restrict__ h_row, f64 pmass,
+                                                     f64 *__restrict__ omega_local) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    u32 a  = rs.row_rank ? rs.row_rank[t] : t;
+    u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    f64 h_a = h_row[t];
+    float sf, sg;
+    density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(1.0 / h_a), sf, sg);
+    f64 sumdWdh = -pmass * kNorm3d * (f64) sg / (h_a * h_a * h_a * h_a);
+    f64 rho_ha  = rho_h64(pmass, h_a);
+    omega_local[rs.row_local ? rs.row_local[t] : t] = 1 + (h_a / (3 * rho_ha)) * sumdWdh;
+}
+
+struct MixedParams {
+    float alpha_u, alpha_AV, beta_AV;
+};
+
+// FP32 pair loop of the constant-AV derivatives; returns the bare sums
+//   F = sum (ca Fa + cb Fb) r_hat   (acceleration = -m F)
+//   U = sum [AVPa c1a Fa (v.r_hat) + 0.5 alpha_u vsig_u (u_a - u_b)(Fa c2a + Fb c2b)]
+//   (du/dt = m U), and the v_sig maximum of the reference's separate v_sig kernel.
+__device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
+                                               u32 k0, u32 k1, const MixedParams &p, float &Fx,
+                                               float &Fy, float &Fz, float &U, float &vsig_max) {
+    float4 Aa = __ldg(&ms.A[a]), Ba = __ldg(&ms.B[a]), Ca = __ldg(&ms.C[a]),
+           Da = __ldg(&ms.D[a]), Ea = __ldg(&ms.E[a]);
+    const float hia = Aa.w, cs_a = Ba.w, u_a = Ca.w, rho_a = Da.w;
+    const float P_a = Ea.x + Ea.y, c1a = Ea.z, c2a = Ea.w;
+    const float k4a = hia * hia * hia * hia * kNorm3dF;
+    const float hia2 = hia * hia;
+    float cx = 0.f, cy = 0.f, cz = 0.f, cu = 0.f;
+    Fx = Fy = Fz = U = 0.f;
+    vsig_max = 0.f;
+    for (u32 k = k0; k < k1; k++) {
+        u32 b     = __ldg(&rs.ent[k]);
+        float4 Ab = __ldg(&ms.A[b]), Bb = __ldg(&ms.B[b]);
+        float dx = (Aa.x - Ab.x) + (Ba.x - Bb.x);
+        float dy = (Aa.y - Ab.y) + (Ba.y - Bb.y);
+        float dz = (Aa.z - Ab.z) + (Ba.z - Bb.z);
+        float r2 = dx * dx + dy * dy + dz * dz;
+        float hib = Ab.w;
+        if ((r2 * hia2 > 4.f && r2 * hib * hib > 4.f) || r2 == 0.f) continue;
+        float4 Cb = __ldg(&ms.C[b]), Db = __ldg(&ms.D[b]), Eb = __ldg(&ms.E[b]);
+        float rinv = rsqrtf(r2);
+        float rab  = r2 * rinv;
+        float Fa   = k4a * m4_df32(rab * hia);
+        float Fb   = hib * hib * hib * hib * kNorm3dF * m4_df32(rab * hib);
+        float rx = dx * rinv, ry = dy * rinv, rz = dz * rinv;
+        float vx = (Ca.x - Cb.x) + (Da.x - Db.x);
+        float vy = (Ca.y - Cb.y) + (Da.y - Db.y);
+        float vz = (Ca.z - Cb.z) + (Da.z - Db.z);
+        float vr  = vx * rx + vy * ry + vz * rz;
+        float avr = fabsf(vr);
+        float rho_b = Db.w, cs_b = Bb.w;
+        float vsig_a = p.alpha_AV * cs_a + p.beta_AV * avr;
+        float vsig_b = p.alpha_AV * cs_b + p.beta_AV * avr;
+        float dP     = (Ea.x - Eb.x) + (Ea.y - Eb.y);
+        float vsig_u = sqrtf(fabsf(dP) / ((rho_a + rho_b) * 0.5f));
+        float qa = fmaxf(-0.5f * rho_a * vsig_a * vr, 0.f);
+        float qb = fmaxf(-0.5f * rho_b * vsig_b * vr, 0.f);
+        float AVPa = P_a + qa, AVPb = (Eb.x + Eb.y) + qb;
+        float f    = AVPa * c1a * Fa + AVPb * Eb.z * Fb;
+        kahan_add(Fx, cx, f * rx);
+        kahan_add(Fy, cy, f * ry);
+        kahan_add(Fz, cz, f * rz);
+        float du = AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - Cb.w) * (Fa * c2a + Fb * Eb.w);
+        kahan_add(U, cu, du);
+        vsig_max = fmaxf(vsig_max, cs_a + 2.f * avr);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_derivs_mixed(RowSpace rs, MixedSpace ms, MixedParams p,
+                                                      f64 pmass, f64 *__restrict__ ax,
+                                                      f64 *__restrict__ ay, f64 *__restrict__ az,
+                                                      f64 *__restrict__ du, f64 *__restrict__ vsig) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    u32 a  = rs.row_rank ? rs.row_rank[t] : t;
+    u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    float Fx, Fy, Fz, U, vm;
+    derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm);
+    ax[t] = -pmass * (f64) Fx;
+    ay[t] = -pmass * (f64) Fy;
+    az[t] = -pmass * (f64) Fz;
+    du[t] = pmass * (f64) U;
+    if (vsig) vsig[t] = (f64) vm;
+}
+
+__global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpace ms,
+                                                           MixedParams p, f64 pmass,
+                                                           const f64 *__restrict__ h_rank, f64 hdt,
+                                                           f64 C_cour, f64 C_force, LocalFields lf,
+                                                           Scalars *sc) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    u64 ev2 = 0, dtm = ~0ull;
+    f64 v2  = 0;
+    if (t < rs.n) {
+        u32 a  = rs.row_rank[t];
+        u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+        float Fx, Fy, Fz, U, vm;
+        derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm);
+        f64 fx = -pmass * (f64) Fx, fy = -pmass * (f64) Fy, fz = -pmass * (f64) Fz;
+        f64 tdu = pmass * (f64) U;
+        u32 i     = rs.row_local[t];
+        size_t iv = (size_t) i * lf.vs;
+        f64 ox = lf.ax[iv], oy = lf.ay[iv], oz = lf.az[iv], odu = lf.du[i];
+        lf.ax[iv] = fx;
+        lf.ay[iv] = fy;
+        lf.az[iv] = fz;
+        lf.du[i]  = tdu;
+        f64 ix = hdt * (fx - ox), iy = hdt * (fy - oy), iz = hdt * (fz - oz);
+        f64 nvx = lf.vx[iv] + ix, nvy = lf.vy[iv] + iy, nvz = lf.vz[iv] + iz;
+        lf.vx[iv] = nvx;
+        lf.vy[iv] = nvy;
+        lf.vz[iv] = nvz;
+        lf.u[i]   = lf.u[i] + hdt * (tdu - odu);
+        ev2       = f64_to_ordered(ix * ix + iy * iy + iz * iz);
+        v2        = nvx * nvx + nvy * nvy + nvz * nvz;
+        f64 h_a   = h_rank[a];
+        f64 dt    = fmin(__longlong_as_double(0x7ff0000000000000ll), C_cour * h_a / (f64) vm);
+        f64 abs_a = sqrt(fx * fx + fy * fy + fz * fz);
+        dt        = fmin(dt, C_force * sqrt(h_a / abs_a));
+        dtm       = f64_to_ordered(dt);
+    }
+    ev2 = block_reduce(ev2, OpMaxU64{}, 0ull);
+    dtm = block_reduce(dtm, OpMinU64{}, ~0ull);
+    v2  = block_reduce(v2, OpAddF64{}, 0.0);
+    if (threadIdx.x == 0) {
+        atomicMax((unsigned long long *) &sc->epsv2_max, (unsigned long long) ev2);
+        atomicMin((unsigned long long *) &sc->dt_min, (unsigned long long) dtm);
+        atomicAdd(&sc->sum_v2, v2);
+    }
+}
+
+MixedSpace mixed_space(Ctx &c, u32 N) {
+    float4 *base = c.f_pos.as<float4>();
+    return MixedSpace{base, base + N, c.f_aux0.as<float4>(), c.f_aux1.as<float4>(),
+                      c.f_aux2.as<float4>()};
+}
+
+cudaError_t ensure_mixed(Ctx &c, u32 N) {
+    cudaError_t e;
+    if ((e = c.f_pos.ensure(2 * sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
+    if ((e = c.f_aux0.ensure(sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
+    if ((e = c.f_aux1.ensure(sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
+    return c.f_aux2.ensure(sizeof(float4) * (size_t) N, c.stream);
+}
+
+} // namespace
+
+cudaError_t stage_positions_mixed(Ctx &c, u32 N) {
+    cudaError_t e = ensure_mixed(c, N);
+    if (e != cudaSuccess) return e;
+    MixedSpace ms = mixed_space(c, N);
+    ProfScope ps(c, kProfTree, N);
+    { k_stage_pos<<<div_up(N, 256), 256, 0, c.stream>>>(N, c.sx.as<f64>(), c.sy.as<f64>(),
+                                                      c.sz.as<f64>(), c.sh.as<f64>(),
+                                                      (float4 *) ms.A, (float4 *) ms.B); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
+                            f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters) {
+    ProfScope ps(c, kProfHIter, rs.n);
+    MixedSpace ms = mixed_space(c, c.n_obj);
+    { k_h_iterate_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(
+        rs, ms, h_old, h_new, eps, pmass, h_evol_max, h_evol_iter_max, iters,
+        c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local) {
+    ProfScope ps(c, kProfOmega, rs.n);
+    MixedSpace ms = mixed_space(c, c.n_obj);
+    { k_omega_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(rs, ms, h_row, pmass, omega_local); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
+                              f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,
+                              f64 C_force, const LocalFields &lf) {
+    u32 N         = c.n_obj;
+    MixedSpace ms = mixed_space(c, N);
+    {
+        ProfScope ps(c, kProfGatherEos, N);
+        { k_stage_hydro<<<div_up(N, 256), 256, 0, c.stream>>>(N, nullptr, nullptr, nullptr, hs, pmass,
+                                                            (float4 *) ms.A, (float4 *) ms.B,
+                                                            (float4 *) ms.C, (float4 *) ms.D,
+                                                            (float4 *) ms.E); GBSPH_COUNTED; }
+    }
+    MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
+    ProfScope ps(c, kProfDerivs, rs.n);
+    { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, hs.h, hdt, C_cour,
+                                                                 C_force, lf,
+                                                                 c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
+                                f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
+                                f64 *du, f64 *vsig) {
+    // merged count = 1 + largest entry; the caller's merged arrays are sized by it
+    u32 N = c.n_obj;
+    cudaError_t e = ensure_mixed(c, N);
+    if (e != cudaSuccess) return e;
+    MixedSpace ms = mixed_space(c, N);
+    { k_stage_hydro<<<div_up(N, 256), 256, 0, c.stream>>>(N, rs.x, rs.y, rs.z, hs, pmass,
+                                                        (float4 *) ms.A, (float4 *) ms.B,
+                                                        (float4 *) ms.C, (float4 *) ms.D,
+                                                        (float4 *) ms.E); GBSPH_COUNTED; }
+    MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
+    { k_derivs_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, ax, ay, az, du, vsig); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+} // namespace gbsph

@@ -1,0 +1,31 @@
+// Mixed-precision (FP32 pair arithmetic) variants of the SPH pair kernels.
+#pragma once
+
+#include "sph_kernels.cuh"
+
+namespace gbsph {
+
+// Rank-ordered FP32 staging of merged fields for the mixed pair kernels, five
+// float4 per particle (80 bytes):
+//   A = {x_hi, y_hi, z_hi, 1/h}      B = {x_lo, y_lo, z_lo, c_s}
+//   C = {vx_hi, vy_hi, vz_hi, u}     D = {vx_lo, vy_lo, vz_lo, rho}
+//   E = {P_hi, P_lo, 1/(rho^2 Omega), 1/(rho Omega)}
+// A position is carried as an unevaluated sum hi + lo of two floats (hi = fl32(x),
+// lo = fl32(x - hi)), so a pair separation (hi_a - hi_b) + (lo_a - lo_b) is accurate
+// to FP32 rounding of the separation itself, wherever the particles sit in the box.
+struct MixedSpace {
+    const float4 *A, *B, *C, *D, *E;
+};
+
+cudaError_t stage_positions_mixed(Ctx &c, u32 N);
+cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
+                            f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters);
+cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
+cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
+                              f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,
+                              f64 C_force, const LocalFields &lf);
+cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
+                                f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
+                                f64 *du, f64 *vsig);
+
+} // namespace gbsph

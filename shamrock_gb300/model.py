@@ -1,0 +1,426 @@
+"""Python mirror of the reference's SPH model interface for the hot path.
+
+Names, argument meaning and error behaviour follow the pybind11 module of the
+reference (shammodels/sph/src/pySPHModel.cpp: get_Model_SPH :1725-1754, the
+SolverConfig setters :107-262, model methods :773-1433), so that scripts written
+for ``shamrock.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")``
+run unchanged on the subset the GB300 path covers: one patch, periodic or free
+box, M4 kernel, constant artificial viscosity, adiabatic EOS.
+
+Particle fields live on the GPU as float64 torch tensors in structure-of-arrays
+layout; every step runs through the C ABI (``libgbsph.so``).  Setup helpers work
+on host numpy arrays until the first step uploads them.
+"""
+
+import json
+import math
+
+import numpy as np
+
+from . import _lib as L
+
+FIELDS_VEC = ("xyz", "vxyz", "axyz")
+FIELDS_SCAL = ("hpart", "uint", "duint")
+
+
+class SolverConfig:
+    """Hot-path subset of shammodels::sph::SolverConfig (SolverConfig.hpp)."""
+
+    def __init__(self):
+        self.gpart_mass = 0.0
+        self.av = dict(type="constant", alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0)
+        self.boundary = "free"
+        self.eos = None
+        self.cfl_cour = 0.0
+        self.cfl_force = 0.0
+        self.cfl_multiplier_stiffness = 2.0
+        self.tree_reduction_level = 3
+        self.use_two_stage_search = True
+        self.htol_up_coarse_cycle = 1.1
+        self.htol_up_fine_cycle = 1.1
+        self.epsilon_h = 1e-6
+        self.h_iter_per_subcycles = 50
+        self.h_max_subcycles_count = 100
+        self.precision = "fp64"
+
+    # -- setters named as the reference's python bindings
+    def set_artif_viscosity_Constant(self, alpha_u, alpha_AV, beta_AV):
+        self.av = dict(type="constant", alpha_u=float(alpha_u), alpha_AV=float(alpha_AV),
+                       beta_AV=float(beta_AV))
+
+    def set_artif_viscosity_VaryingMM97(self, **kw):
+        raise NotImplementedError("only constant artificial viscosity is on the GB300 path")
+
+    def set_artif_viscosity_VaryingCD10(self, **kw):
+        raise NotImplementedError("only constant artificial viscosity is on the GB300 path")
+
+    def set_boundary_periodic(self):
+        self.boundary = "periodic"
+
+    def set_boundary_free(self):
+        self.boundary = "free"
+
+    def set_eos_adiabatic(self, gamma):
+        self.eos = dict(type="adiabatic", gamma=float(gamma))
+
+    def set_particle_mass(self, pmass):
+        self.gpart_mass = float(pmass)
+
+    def set_tree_reduction_level(self, level):
+        self.tree_reduction_level = int(level)
+
+    def set_two_stage_search(self, enable):
+        # the one- and two-stage searches produce the same pair set in the same order
+        self.use_two_stage_search = bool(enable)
+
+    def set_cfl_cour(self, v):
+        self.cfl_cour = float(v)
+
+    def set_cfl_force(self, v):
+        self.cfl_force = float(v)
+
+    def set_cfl_mult_stiffness(self, v):
+        self.cfl_multiplier_stiffness = float(v)
+
+    def set_smoothing_length_density_based(self):
+        pass
+
+    def set_precision(self, precision):
+        """"fp64" (bit-identical to the FP64 oracle) or "mixed" (FP32 pair arithmetic)."""
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
+
+    def to_dict(self):
+        return dict(self.__dict__)
+
+    def print_status(self):
+        print(json.dumps(self.to_dict(), indent=1))
+
+
+class Context:
+    """Stand-in for shamrock.Context: holds the model attached to it."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self.model = None
+
+    def pdata_layout_new(self):
+        pass
+
+    def collect_data(self):
+        if self.model is None:
+            raise RuntimeError("no model attached to this context")
+        return self.model.collect_data()
+
+
+def get_Model_SPH(context, vector_type="f64_3", sph_kernel="M4"):
+    """shamrock.get_Model_SPH (pySPHModel.cpp:1725-1754)."""
+    if vector_type != "f64_3":
+        raise ValueError(f"unknown vector type {vector_type}: the SPH solver is instantiated "
+                         "for f64_3 only (Solver.cpp:3276-3282)")
+    if sph_kernel != "M4":
+        raise ValueError(f"kernel {sph_kernel} is not on the GB300 path (M4 only)")
+    m = Model(context)
+    context.model = m
+    return m
+
+
+class Model:
+    """shammodels::sph::Model<f64_3, M4> for one patch on one GB300."""
+
+    def __init__(self, context):
+        self.ctx_py = context
+        self.cfg = SolverConfig()
+        self.box_min = np.zeros(3)
+        self.box_max = np.ones(3)
+        self._host = {k: np.zeros((0, 3)) for k in FIELDS_VEC}
+        self._host.update({k: np.zeros(0) for k in FIELDS_SCAL})
+        self._dev = None  # dict of torch tensors once uploaded
+        self._omega = None
+        self.time = 0.0
+        self.dt = 0.0
+        self.cfl_mult = 1e-2
+        self.logs = []
+        self._lib_ctx = None
+        self.scheduler = (None, None)
+
+    # ------------------------------------------------------------------ config
+    def gen_default_config(self):
+        return SolverConfig()
+
+    def set_solver_config(self, cfg):
+        self.cfg = cfg
+
+    def get_solver_config(self):
+        return self.cfg
+
+    def init_scheduler(self, crit_split, crit_merge):
+        self.scheduler = (crit_split, crit_merge)
+
+    def resize_simulation_box(self, box_min, box_max):
+        self.box_min = np.asarray(box_min, float)
+        self.box_max = np.asarray(box_max, float)
+
+    def set_particle_mass(self, pmass):
+        self.cfg.set_particle_mass(pmass)
+
+    def get_particle_mass(self):
+        return self.cfg.gpart_mass
+
+    def set_cfl_cour(self, v):
+        self.cfg.set_cfl_cour(v)
+
+    def set_cfl_force(self, v):
+        self.cfg.set_cfl_force(v)
+
+    def set_cfl_mult_stiffness(self, v):
+        self.cfg.set_cfl_mult_stiffness(v)
+
+    def get_hfact(self):
+        return 1.2
+
+    def rho_h(self, h):
+        return self.cfg.gpart_mass * (self.get_hfact() / np.asarray(h)) ** 3
+
+    def total_mass_to_part_mass(self, totmass):
+        n = self.get_total_part_count()
+        if n == 0:
+            raise RuntimeError("no particles")
+        return totmass / n
+
+    # ------------------------------------------------------------------ particles (setup)
+    def get_total_part_count(self):
+        if self._dev is not None:
+            return int(self._dev["hpart"].shape[0])
+        return int(self._host["hpart"].shape[0])
+
+    def push_particle(self, pos, hpart, upart):
+        self._to_host()
+        pos = np.asarray(pos, float).reshape(-1, 3)
+        n = pos.shape[0]
+        self._host["xyz"] = np.concatenate([self._host["xyz"], pos])
+        self._host["vxyz"] = np.concatenate([self._host["vxyz"], np.zeros((n, 3))])
+        self._host["axyz"] = np.concatenate([self._host["axyz"], np.zeros((n, 3))])
+        self._host["hpart"] = np.concatenate([self._host["hpart"], np.asarray(hpart, float)])
+        self._host["uint"] = np.concatenate([self._host["uint"], np.asarray(upart, float)])
+        self._host["duint"] = np.concatenate([self._host["duint"], np.zeros(n)])
+
+    def add_cube_fcc_3d(self, dr, box_min, box_max):
+        """Close-packed lattice of the reference's add_particles_fcc
+        (shammodels/common/include/shammodels/common/setup/generators.hpp:82-127), keeping
+        the sites inside the half-open box; h = 2 dr (the reference pushes r_particle and the
+        model later rescales by hfact)."""
+        bmin = np.asarray(box_min, float)
+        bmax = np.asarray(box_max, float)
+        dim = (bmax - bmin) / np.array([2.0, math.sqrt(3.0), 2.0 * math.sqrt(6.0) / 3.0]) / dr
+        ix, iy, iz = (int(math.ceil(v)) for v in dim)
+        i, j, k = np.meshgrid(np.arange(ix), np.arange(iy), np.arange(iz), indexing="ij")
+        i, j, k = i.ravel(), j.ravel(), k.ravel()
+        pos = np.stack([2 * i + ((j + k) % 2),
+                        math.sqrt(3.0) * (j + (1.0 / 3.0) * (k % 2)),
+                        2 * math.sqrt(6.0) * k / 3.0], 1) * dr + bmin
+        keep = np.all((pos >= bmin) & (pos < bmax), axis=1)
+        pos = pos[keep]
+        self.push_particle(pos, np.full(len(pos), 2 * dr), np.zeros(len(pos)))
+
+    def set_particles(self, pos, vel=None, h=None, u=None):
+        """Replace all particles (host arrays); h defaults to hfact*(m/rho=1)^(1/3)."""
+        pos = np.asarray(pos, float).reshape(-1, 3)
+        n = pos.shape[0]
+        self._dev = None
+        self._host = dict(
+            xyz=pos.copy(), vxyz=np.zeros((n, 3)) if vel is None else np.asarray(vel, float).copy(),
+            axyz=np.zeros((n, 3)),
+            hpart=np.full(n, 1.2 * (1.0 / n) ** (1 / 3)) if h is None else np.asarray(h, float).copy(),
+            uint=np.zeros(n) if u is None else np.asarray(u, float).copy(), duint=np.zeros(n))
+
+    def _field_host(self, name):
+        self._to_host()
+        return self._host[name]
+
+    def set_value_in_a_box(self, field_name, field_type, value, box_min, box_max, ivar=0):
+        self._to_host()
+        pos = self._host["xyz"]
+        sel = np.all((pos >= np.asarray(box_min)) & (pos < np.asarray(box_max)), axis=1)
+        self._host[field_name][sel] = value
+
+    def add_kernel_value(self, field_name, field_type, value, center, h_ker):
+        """Adds value * W_M4(|r - center|, h_ker) / W_M4(0, h_ker) ... as the reference's
+        add_kernel_value: value times the normalised M4 kernel at each particle."""
+        self._to_host()
+        r = np.linalg.norm(self._host["xyz"] - np.asarray(center, float), axis=1)
+        q = r / h_ker
+        f = np.where(q < 1, 0.25 * (2 - q) ** 3 - (1 - q) ** 3, np.where(q < 2, 0.25 * (2 - q) ** 3, 0))
+        self._host[field_name] += value * f / (math.pi * h_ker**3)
+
+    def get_sum(self, field_name, field_type):
+        self._to_host()
+        return float(np.sum(self._host[field_name]))
+
+    # ------------------------------------------------------------------ device data
+    def _lib(self):
+        if self._lib_ctx is None:
+            self._lib_ctx = L.Context(self.ctx_py.device if self.ctx_py else 0)
+        return self._lib_ctx
+
+    def _to_device(self):
+        import torch
+
+        if self._dev is not None:
+            return self._dev
+        dev = torch.device("cuda", self.ctx_py.device if self.ctx_py else 0)
+        d = {}
+        for k in FIELDS_VEC:
+            d[k] = torch.as_tensor(np.ascontiguousarray(self._host[k].T), device=dev).contiguous()
+        for k in FIELDS_SCAL:
+            d[k] = torch.as_tensor(self._host[k], device=dev).contiguous()
+        d["omega"] = torch.ones_like(d["hpart"])
+        self._dev = d
+        return d
+
+    def _to_host(self):
+        if self._dev is None:
+            return
+        for k in FIELDS_VEC:
+            self._host[k] = self._dev[k].T.cpu().numpy().copy()
+        for k in FIELDS_SCAL:
+            self._host[k] = self._dev[k].cpu().numpy().copy()
+        self._omega = self._dev["omega"].cpu().numpy().copy()
+        self._dev = None
+
+    def get_field_tensor(self, name):
+        """Device tensor of a field: (3, N) for vectors, (N,) for scalars (torch binding)."""
+        return self._to_device()[name]
+
+    def collect_data(self):
+        """Host copy of the particle fields, keyed as the reference's ctx.collect_data()."""
+        if self._dev is not None:
+            out = {k: self._dev[k].T.cpu().numpy().copy() for k in FIELDS_VEC}
+            out.update({k: self._dev[k].cpu().numpy().copy() for k in FIELDS_SCAL})
+            out["omega"] = self._dev["omega"].cpu().numpy().copy()
+            return out
+        out = {k: v.copy() for k, v in self._host.items()}
+        if self._omega is not None:
+            out["omega"] = self._omega.copy()
+        return out
+
+    def _particles_struct(self):
+        d = self._to_device()
+        n = d["hpart"].shape[0]
+        p = L.Particles()
+        p.n = n
+        for k in FIELDS_VEC:
+            t = d[k]
+            v = L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0)
+            setattr(p, k, v)
+        p.hpart = d["hpart"].data_ptr()
+        p.uint = d["uint"].data_ptr()
+        p.duint = d["duint"].data_ptr()
+        p.omega = d["omega"].data_ptr()
+        return p
+
+    def _config_struct(self):
+        c = self.cfg
+        if c.eos is None or c.eos["type"] != "adiabatic":
+            raise RuntimeError("set_eos_adiabatic must be called: only the adiabatic EOS is on "
+                               "the GB300 path")
+        if c.gpart_mass == 0:
+            raise RuntimeError(f"invalid gpart_mass {c.gpart_mass}, this configuration can not "
+                               "converge.\nPlease set it using either model.set_particle_mass(pmass)"
+                               " or cfg.set_particle_mass(pmass)")
+        s = L.Config()
+        s.gamma = c.eos["gamma"]
+        s.pmass = c.gpart_mass
+        s.alpha_u, s.alpha_AV, s.beta_AV = c.av["alpha_u"], c.av["alpha_AV"], c.av["beta_AV"]
+        s.cfl_cour, s.cfl_force = c.cfl_cour, c.cfl_force
+        s.cfl_mult_stiffness = c.cfl_multiplier_stiffness
+        s.htol_up_coarse, s.htol_up_fine = c.htol_up_coarse_cycle, c.htol_up_fine_cycle
+        s.epsilon_h = c.epsilon_h
+        s.h_iter_per_subcycles = c.h_iter_per_subcycles
+        s.h_max_subcycles = c.h_max_subcycles_count
+        s.tree_reduction_level = c.tree_reduction_level
+        s.periodic = 1 if c.boundary == "periodic" else 0
+        s.box_min = L.d3(self.box_min)
+        s.box_max = L.d3(self.box_max)
+        s.precision = L.GBSPH_MIXED if c.precision == "mixed" else L.GBSPH_FP64
+        return s
+
+    # ------------------------------------------------------------------ time stepping
+    def evolve_once(self, stream=None):
+        """Solver::evolve_once (Solver.cpp:1942-3272) on the GPU; returns the step log."""
+        lib = self._lib()
+        p = self._particles_struct()
+        cfg = self._config_struct()
+        ts = L.TimeState(self.time, self.dt, self.cfl_mult)
+        log = L.StepLog()
+        import ctypes as C
+
+        rc = lib.lib.gbsph_evolve_once(lib.handle, C.byref(p), C.byref(cfg), C.byref(ts),
+                                       C.byref(log), stream)
+        lib.check(rc)
+        self.time, self.dt, self.cfl_mult = ts.t, ts.dt, ts.cfl_mult
+        d = log.as_dict()
+        self.logs.append(d)
+        return d
+
+    def timestep(self):
+        return self.evolve_once()
+
+    def evolve_once_override_time(self, t_current, dt_input):
+        self.time = float(t_current)
+        self.dt = float(dt_input)
+        self.evolve_once()
+        return self.dt
+
+    def evolve_until(self, target_time, niter_max=-1):
+        it = 0
+        while self.time < target_time:
+            if niter_max >= 0 and it >= niter_max:
+                return False
+            if self.time + self.dt > target_time:
+                self.dt = target_time - self.time
+            self.evolve_once()
+            it += 1
+        return True
+
+    def get_time(self):
+        return self.time
+
+    def get_dt(self):
+        return self.dt
+
+    def set_next_dt(self, dt):
+        self.dt = float(dt)
+
+    def set_time(self, t):
+        self.time = float(t)
+
+    def set_cfl_multipler(self, m):
+        self.cfl_mult = float(m)
+
+    def get_cfl_multipler(self):
+        return self.cfl_mult
+
+    def solver_logs_last_rate(self):
+        return self.logs[-1]["rate"] if self.logs else 0.0
+
+    def solver_logs_last_obj_count(self):
+        return self.logs[-1]["n_local"] if self.logs else 0
+
+    def solver_logs_step_count(self):
+        return len(self.logs)
+
+    # ------------------------------------------------------------------ analysis (FP64 totals)
+    def get_kinetic_energy(self):
+        d = self._to_device()
+        v = d["vxyz"]
+        return float(0.5 * self.cfg.gpart_mass * (v * v).sum().item())
+
+    def get_total_momentum(self):
+        d = self._to_device()
+        return tuple((self.cfg.gpart_mass * d["vxyz"].sum(dim=1)).cpu().numpy().tolist())
+
+    def get_thermal_energy(self):
+        d = self._to_device()
+        return float(self.cfg.gpart_mass * d["uint"].sum().item())

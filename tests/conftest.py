@@ -13,6 +13,21 @@ def pytest_configure(config):
 
 
 @pytest.fixture(scope="session")
+def gctx():
+    """A library context on cuda:0.  GPU tests fail (not skip) without a device: the
+    CUDA path is the only path."""
+    import torch
+
+    from shamrock_gb300 import _lib
+
+    assert torch.cuda.is_available(), "GPU test run without a CUDA device"
+    torch.cuda.init()
+    ctx = _lib.Context(0)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="session")
 def golden():
     import json
 

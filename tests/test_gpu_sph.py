@@ -1,0 +1,159 @@
+"""GPU parity of the SPH modules (h-rho Newton iteration, Omega, EOS, constant-AV
+derivatives, v_sig) against the reference golden vectors and the oracle.
+
+FP64 results are required to be bit-identical to the oracle (same evaluation order,
+FMA off).  The mixed-precision derivatives are checked against the FP64 ones with the
+tolerances of the FP32-mixed mode: max relative error of |a| and du/dt, normalised by
+the largest magnitude of the field, <= 1e-5."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M():
+    from shamrock_gb300 import modules
+
+    return modules
+
+
+def test_golden_h_iteration_gpu(gctx, M, golden):
+    """IterateSmoothingLengthDensityTests.cpp:250-366 replayed through gbsph_h_iterate."""
+    g = golden("h_iteration.json")["tests"]["shammodels/sph/modules/IterateSmoothingLengthDensity"]
+    v, c = g["vectors"], g["constants"]
+    pos = np.array([[i, j, k] for i in range(4) for j in range(4) for k in range(4)], float)
+    n = len(pos)
+    csr = M.csr_to_cuda(dict(cnt=np.full(n, n), scanned=np.arange(n) * n,
+                             entries=np.tile(np.arange(n), n)))
+    h_new = torch.full((n,), 0.1, dtype=torch.float64, device="cuda")
+    eps = torch.full((n,), 1e7, dtype=torch.float64, device="cuda")
+    seq = {"eps_min": [], "eps_max": [], "h_min": [], "h_max": []}
+    for outer in range(50):
+        h_old = h_new.clone()
+        eps.fill_(1e7)
+        max_eps = 1e7
+        for inner in range(10):
+            mx, mn, _ = M.h_iterate(gctx, csr, pos, h_old, h_new, eps, c["gpart_mass"],
+                                    c["h_evol_max"], c["h_evol_iter_max"], 1)
+            seq["eps_min"].append(mn)
+            seq["eps_max"].append(mx)
+            seq["h_min"].append(h_new.min().item())
+            seq["h_max"].append(h_new.max().item())
+            max_eps = mx
+            if max_eps < 1e-6:
+                break
+        if mn == -1:
+            continue
+        if max_eps < 1e-6:
+            break
+    np.testing.assert_allclose(h_new.cpu().numpy(), v["expected_h_vec_end"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(eps.cpu().numpy(), v["expected_eps_vec_end"], rtol=0, atol=1e-6)
+    for k in seq:
+        np.testing.assert_allclose(seq[k], v["expected_sequence_" + k], rtol=0, atol=1e-6)
+
+
+@pytest.fixture(scope="module")
+def scene():
+    """Jittered Sedov lattice with random velocities, its ghosts, tree, cache (oracle),
+    converged-ish h (one oracle Newton pass) and merged hydro fields."""
+    from shamrock_gb300 import setups
+
+    s = setups.sedov_taylor(8, jitter=0.05, seed=11)
+    rng = np.random.default_rng(2)
+    n = len(s["h"])
+    vel = rng.normal(0, 0.1, size=(n, 3))
+    src, off = O.periodic_ghosts(s["pos"], s["h"], [0, 0, 0], [1, 1, 1], 1.1)
+    mpos = np.concatenate([s["pos"], s["pos"][src] + off])
+    mh = np.concatenate([s["h"], s["h"][src]])
+    lo, hi = np.nextafter(mpos.min(0), -np.inf), np.nextafter(mpos.max(0), np.inf)
+    t = O.Tree(mpos, lo, hi, 3, h=mh, htol=1.1)
+    csr = t.neigh_cache(mpos, mh, n, 1.1)
+    h_new, eps = s["h"].copy(), np.full(n, 100.0)
+    O.h_iterate_once(csr, mpos, s["h"], h_new, eps, s["pmass"], 1.1, 1.1)
+    om = O.omega(csr, mpos, h_new, s["pmass"])
+    m = lambda f: np.concatenate([f, f[src]])
+    fields = dict(pos=mpos, v=m(vel), h=m(h_new), om=m(om), u=m(s["u"]), h_old=s["h"],
+                  h_iter=h_new, eps=eps)
+    P, cs = O.eos_adiabatic(fields["h"], fields["u"], s["pmass"], s["gamma"])
+    fields.update(P=P, cs=cs)
+    return dict(s=s, csr=csr, f=fields, n=n)
+
+
+def test_h_iterate_once_bitexact(gctx, M, scene):
+    s, f, n = scene["s"], scene["f"], scene["n"]
+    csr = M.csr_to_cuda(scene["csr"])
+    h_new = torch.as_tensor(s["h"].copy(), device="cuda")
+    eps = torch.full((n,), 100.0, dtype=torch.float64, device="cuda")
+    M.h_iterate(gctx, csr, f["pos"], torch.as_tensor(s["h"], device="cuda"), h_new, eps,
+                s["pmass"], 1.1, 1.1, 1)
+    assert np.array_equal(h_new.cpu().numpy(), f["h_iter"])
+    assert np.array_equal(eps.cpu().numpy(), f["eps"])
+
+
+def test_h_iterate_fused_equals_global_loop(gctx, M, scene):
+    """Per-particle fused Newton loop == the reference's global loop (epsilon_h = 1e-6)."""
+    s, f, n = scene["s"], scene["f"], scene["n"]
+    csr = M.csr_to_cuda(scene["csr"])
+    h0 = torch.as_tensor(s["h"], device="cuda")
+    # global loop, one iteration per call
+    hg = h0.clone()
+    eg = torch.full((n,), 100.0, dtype=torch.float64, device="cuda")
+    for it in range(50):
+        mx, mn, _ = M.h_iterate(gctx, csr, f["pos"], h0, hg, eg, s["pmass"], 1.1, 1.1, 1)
+        if mx < 1e-6:
+            break
+    hf = h0.clone()
+    ef = torch.full((n,), 100.0, dtype=torch.float64, device="cuda")
+    M.h_iterate(gctx, csr, f["pos"], h0, hf, ef, s["pmass"], 1.1, 1.1, 50)
+    assert torch.equal(hg, hf) and torch.equal(eg, ef)
+
+
+def test_omega_eos_bitexact(gctx, M, scene):
+    s, f, n = scene["s"], scene["f"], scene["n"]
+    csr = M.csr_to_cuda(scene["csr"])
+    om = M.omega(gctx, csr, f["pos"], f["h_iter"], s["pmass"])
+    assert np.array_equal(om.cpu().numpy(), f["om"][:n])
+    P, cs = M.eos_adiabatic(gctx, f["h"], f["u"], s["pmass"], s["gamma"])
+    assert np.array_equal(P.cpu().numpy(), f["P"])
+    assert np.array_equal(cs.cpu().numpy(), f["cs"])
+
+
+def test_derivs_vsig_fp64_bitexact(gctx, M, scene):
+    s, f, n = scene["s"], scene["f"], scene["n"]
+    csr = M.csr_to_cuda(scene["csr"])
+    a, du, vs = M.derivs_constAV(gctx, csr, f["pos"], f["v"], f["h"], f["om"], f["u"], f["P"],
+                                 f["cs"], s["pmass"], 1.0, 1.0, 2.0)
+    oa, odu = O.derivs_constAV(scene["csr"], f["pos"], f["v"], f["h"], f["om"], f["u"], f["P"],
+                               f["cs"], s["pmass"], 1.0, 1.0, 2.0)
+    ovs = O.vsig(scene["csr"], f["pos"], f["v"], f["h"], f["cs"])
+    assert np.array_equal(a.T.cpu().numpy(), oa)
+    assert np.array_equal(du.cpu().numpy(), odu)
+    assert np.array_equal(vs.cpu().numpy(), ovs)
+
+
+def rel_err(x, ref):
+    """max |x - ref| / max |ref| and rms |x - ref| / rms |ref| over particles."""
+    x, ref = np.asarray(x), np.asarray(ref)
+    d = np.abs(x - ref).reshape(len(ref), -1).max(1) if x.ndim > 1 else np.abs(x - ref)
+    r = np.abs(ref).reshape(len(ref), -1).max(1) if ref.ndim > 1 else np.abs(ref)
+    return d.max() / r.max(), np.sqrt(np.mean(d**2) / np.mean(r**2))
+
+
+def test_derivs_mixed_within_tolerance(gctx, M, scene):
+    s, f, n = scene["s"], scene["f"], scene["n"]
+    csr = M.csr_to_cuda(scene["csr"])
+    a64, du64, vs64 = M.derivs_constAV(gctx, csr, f["pos"], f["v"], f["h"], f["om"], f["u"],
+                                       f["P"], f["cs"], s["pmass"], 1.0, 1.0, 2.0)
+    a32, du32, vs32 = M.derivs_constAV(gctx, csr, f["pos"], f["v"], f["h"], f["om"], f["u"],
+                                       f["P"], f["cs"], s["pmass"], 1.0, 1.0, 2.0,
+                                       precision="mixed")
+    tol = 1e-5
+    ea = rel_err(a32.T.cpu().numpy(), a64.T.cpu().numpy())
+    ed = rel_err(du32.cpu().numpy(), du64.cpu().numpy())
+    ev = rel_err(vs32.cpu().numpy(), vs64.cpu().numpy())
+    assert ea[0] <= tol and ed[0] <= tol and ev[0] <= tol, (ea, ed, ev)
