@@ -24,13 +24,12 @@ def _cuda(a, dtype):
 
 
 def soa(pos):
-    """(N, 3) array/tensor -> (3, N) float64 CUDA tensor."""
-    t = _cuda(pos, torch.float64)
-    if t.dim() == 2 and t.shape[1] == 3 and t.shape[0] != 3:
-        t = t.T.contiguous()
-    elif t.dim() == 2 and t.shape == (3, 3):
-        raise ValueError("ambiguous 3x3 positions: pass (3, N)")
-    return t.contiguous()
+    """Positions as a (3, N) float64 CUDA tensor.  Host arrays and lists are read as
+    (N, 3) rows; torch tensors are taken to be (3, N) already."""
+    if isinstance(pos, torch.Tensor):
+        return pos.to(device="cuda", dtype=torch.float64).contiguous()
+    a = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    return torch.as_tensor(np.ascontiguousarray(a.T), device="cuda")
 
 
 _KEY = {32: torch.int32, 64: torch.int64}
