@@ -196,6 +196,30 @@ int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *sc
                          double *ax, double *ay, double *az, double *du, double *vsig,
                          void *stream);
 
+/* Allocation-free variant of gbsph_derivs_constAV(..., GBSPH_MIXED, ...) for callers
+ * that may not allocate device memory (a framework whose pool owns all device memory,
+ * a loop that must not allocate once running) and so cannot hold a gbsph_ctx.  It has
+ * no counterpart in the reference.  Needs no context: it runs on the current device
+ * and takes the same inputs, outputs and results as the context entry point.
+ *  - The FP32 staging lives in a fixed device array inside the library, sized for at
+ *    most 65,536 merged particles (5 MiB, reserved on every GPU that loads the library
+ *    until the process exits); larger n_merged returns GBSPH_ERR_CAPACITY.
+ *  - The first call on a device looks the array's device address up; make that first
+ *    call before any stream capture.
+ *  - All calls share the one array: calls that overlap on the GPU (other streams, other
+ *    threads) race; serialise them.  Nothing needs clearing between calls.
+ *  - Asynchronous on `stream`; returns GBSPH_OK, GBSPH_ERR_CAPACITY, GBSPH_ERR_ARG or
+ *    GBSPH_ERR_CUDA (there is no context to hold a message). */
+int gbsph_derivs_constAV_mixed_noalloc(const uint32_t *cnt, const uint32_t *scanned,
+                                       const uint32_t *entries, const double *x, const double *y,
+                                       const double *z, const double *vx, const double *vy,
+                                       const double *vz, const double *h, const double *omega,
+                                       const double *u, const double *P, const double *cs,
+                                       uint32_t n_local, uint32_t n_merged, double pmass,
+                                       double alpha_u, double alpha_AV, double beta_AV,
+                                       double *ax, double *ay, double *az, double *du,
+                                       double *vsig, void *stream);
+
 /* Periodic ghost layer of one patch covering [bmin, bmax]
  * (BasicSPHGhostHandler::find_interfaces + gen_id_table_interfaces +
  * build_comm_merge_positions, shammodels/sph/src/BasicSPHGhosts.cpp:260-360,512-530).

@@ -83,6 +83,8 @@ SIGNATURES = {
     "gbsph_derivs_constAV": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _vp, _vp, _vp, _u32, _u32, _f64, _f64, _f64, _f64,
                                        _u32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbsph_derivs_constAV_mixed_noalloc": (C.c_int, [_vp] * 14 + [_u32, _u32, _f64, _f64, _f64,
+                                                                   _f64] + [_vp] * 6),
     "gbsph_periodic_ghosts": (C.c_int, [_vp, Vec3, _vp, _u32, _P(_f64), _P(_f64), _f64, _P(_u32),
                                         _vp]),
     "gbsph_ghost_export": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

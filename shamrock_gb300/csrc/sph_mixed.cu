@@ -361,4 +361,57 @@ cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- allocation-free variant
+// For callers that cannot allocate device memory: a host framework whose own pool owns
+// every device byte, a solver loop that must not allocate once it is running, code that
+// runs where the CUDA allocator may not be called.  They cannot create a gbsph_ctx (its
+// scratch arena is allocated), so this entry point keeps the FP32 staging of the
+// mixed-precision derivatives in a fixed device array that is part of the library image.
+namespace {
+
+// Largest merged (locals + ghosts) particle count the fixed staging holds.
+constexpr u32 kNoAllocMaxMerged = 1u << 16;
+// Five float4 per merged particle: 65,536 x 80 B = 5 MiB, reserved on every GPU that
+// loads the library and kept until the process exits.
+static __device__ __align__(256) float4 g_noalloc_staging[5 * kNoAllocMaxMerged];
+
+constexpr int kNoAllocMaxDevices = 64;
+float4 *g_noalloc_base[kNoAllocMaxDevices] = {};
+
+} // namespace
+
 } // namespace gbsph
+
+extern "C" int gbsph_derivs_constAV_mixed_noalloc(
+    const uint32_t *cnt, const uint32_t *scanned, const uint32_t *entries, const double *x,
+    const double *y, const double *z, const double *vx, const double *vy, const double *vz,
+    const double *h, const double *omega, const double *u, const double *P, const double *cs,
+    uint32_t n_local, uint32_t n_merged, double pmass, double alpha_u, double alpha_AV,
+    double beta_AV, double *ax, double *ay, double *az, double *du, double *vsig, void *stream) {
+    using namespace gbsph;
+    if (n_merged > kNoAllocMaxMerged) return GBSPH_ERR_CAPACITY; // beyond the fixed staging
+    if (n_local > n_merged) return GBSPH_ERR_ARG;
+    if (n_local == 0) return GBSPH_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GBSPH_ERR_CUDA;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return GBSPH_ERR_ARG;
+    // Set-up, once per device, with that device current: the array's name in host code
+    // is only a host-side handle, the kernels need its device address.
+    if (!g_noalloc_base[dev]) {
+        void *p       = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_staging);
+        if (e != cudaSuccess || !p) return GBSPH_ERR_CUDA;
+        g_noalloc_base[dev] = (float4 *) p;
+    }
+    float4 *b     = g_noalloc_base[dev];
+    u32 N         = n_merged;
+    MixedSpace ms{b, b + N, b + 2 * (size_t) N, b + 3 * (size_t) N, b + 4 * (size_t) N};
+    RowSpace rs{n_local, nullptr, nullptr, cnt, scanned, entries, x, y, z};
+    HydroSpace hs{h, u, vx, vy, vz, omega, P, cs};
+    cudaStream_t s = (cudaStream_t) stream;
+    // every staging entry the pair kernel reads is rewritten first: nothing to clear
+    { k_stage_hydro<<<div_up(N, 256), 256, 0, s>>>(N, x, y, z, hs, pmass, b, b + N, b + 2 * (size_t) N, b + 3 * (size_t) N, b + 4 * (size_t) N); GBSPH_COUNTED; }
+    MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
+    { k_derivs_mixed<<<div_up(n_local, 128), 128, 0, s>>>(rs, ms, p, pmass, ax, ay, az, du, vsig); GBSPH_COUNTED; }
+    return cudaGetLastError() == cudaSuccess ? GBSPH_OK : GBSPH_ERR_CUDA;
+}
