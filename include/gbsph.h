@@ -150,8 +150,11 @@ int gbsph_tree_query(gbsph_ctx *ctx, const double *qx, const double *qy, const d
  * positions of the last gbsph_build_tree call (built with h).  Pair test
  * !(r^2 > (h_a htol)^2 R^2 && r^2 > (h_b htol)^2 R^2), R = 2.
  * Replaces NeighbourCache::start_neighbors_cache_2stages,
- * shammodels/sph/src/modules/NeighbourCache.cpp:223-596. */
-int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, void *stream);
+ * shammodels/sph/src/modules/NeighbourCache.cpp:223-596.  With GBSPH_MIXED the pair
+ * test is first estimated in FP32 and only pairs within 1e-5 of the threshold are
+ * decided in FP64: the cache is identical, the work mostly FP32. */
+int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, uint32_t precision,
+                          void *stream);
 
 int gbsph_cache_size(gbsph_ctx *ctx, uint64_t *total_host, uint64_t *leaf_total_host);
 

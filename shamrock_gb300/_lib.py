@@ -73,7 +73,7 @@ SIGNATURES = {
     "gbsph_tree_export": (C.c_int, [_vp] * 13 + [_vp]),
     "gbsph_tree_query": (C.c_int, [_vp, _vp, _vp, _vp, _u32, C.c_int, _f64, _vp, _vp, _u64,
                                    _P(_u64), _vp]),
-    "gbsph_neighbour_cache": (C.c_int, [_vp, _u32, _f64, _vp]),
+    "gbsph_neighbour_cache": (C.c_int, [_vp, _u32, _f64, _u32, _vp]),
     "gbsph_cache_size": (C.c_int, [_vp, _P(_u64), _P(_u64)]),
     "gbsph_cache_export": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "gbsph_h_iterate": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u32, _f64,

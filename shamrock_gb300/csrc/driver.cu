@@ -57,7 +57,7 @@ Ctx::~Ctx() {
     for (cudaEvent_t e : prof.pool) cudaEventDestroy(e);
     DevBuf *bufs[] = {&scan_scratch, &d_scalars, &d_bbox, &keys, &sort_index, &flags_a, &flags_b,
                       &offsets, &reduc, &reduced, &lchild, &rchild, &lflag, &rflag, &endrange,
-                      &parent, &boxes, &visit, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
+                      &parent, &boxes, &visit, &fboxes, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
                       &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
                       &owner, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
@@ -320,15 +320,23 @@ int gbsph_tree_query(gbsph_ctx *ctx, const double *qx, const double *qy, const d
     return GBSPH_OK;
 }
 
-int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, void *stream) {
+int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, uint32_t precision,
+                          void *stream) {
     ENTER(ctx, stream);
     Ctx &c = ctx->c;
     if (c.leaf_count == 0 || !c.has_rint || c.key_bits != 32)
         return fail(ctx, GBSPH_ERR_STATE, "neighbour cache needs a 32-bit tree built with h");
     REQUIRE_ARG(n_local <= c.n_obj, "n_local > merged count");
+    REQUIRE_ARG(precision == GBSPH_FP64 || precision == GBSPH_MIXED, "unknown precision");
     CU(cudaMemsetAsync(c.d_scalars.p, 0, sizeof(Scalars), c.stream));
     CU(build_rows(c, n_local));
-    CU(neigh_cache_build(c, htol));
+    if (precision == GBSPH_MIXED) {
+        CU(stage_positions_mixed(c, c.n_obj, htol));
+        const float4 *fA = c.f_pos.as<float4>();
+        CU(neigh_cache_build(c, htol, fA, fA + c.n_obj));
+    } else {
+        CU(neigh_cache_build(c, htol));
+    }
     CU(cudaStreamSynchronize(c.stream));
     return GBSPH_OK;
 }
@@ -504,8 +512,13 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
         CU(tree_build(c, c.mx.as<f64>(), c.my.as<f64>(), c.mz.as<f64>(), c.mh.as<f64>(), N,
                       cfg->tree_reduction_level, cfg->htol_up_coarse, 32, 0));
         CU(build_rows(c, n));
-        CU(neigh_cache_build(c, cfg->htol_up_coarse));
-        if (mixed) CU(stage_positions_mixed(c, N));
+        if (mixed) {
+            CU(stage_positions_mixed(c, N, cfg->htol_up_coarse));
+            const float4 *fA = c.f_pos.as<float4>();
+            CU(neigh_cache_build(c, cfg->htol_up_coarse, fA, fA + N));
+        } else {
+            CU(neigh_cache_build(c, cfg->htol_up_coarse));
+        }
         rs = RowSpace{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
                       c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
                       c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
@@ -602,7 +615,7 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
         }
         corr_iters++;
     } while (rerun);
-    if (c.h_scalars->flags)
+    if (c.h_scalars->flags & (kFlagStackOverflow | kFlagOwnerMissing | kFlagCsrOverflow))
         return fail(ctx, GBSPH_ERR_CUDA, "kernel error flags raised during the step");
 
     auto t_end    = std::chrono::steady_clock::now();

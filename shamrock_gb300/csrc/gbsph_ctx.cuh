@@ -42,6 +42,13 @@ enum KernelFlags : u32 {
     kFlagStackOverflow = 1u,
     kFlagOwnerMissing  = 2u,
     kFlagCsrOverflow   = 4u,
+    kFlagLeafCap       = 8u, // a leaf had more stage-1 candidates than the one-pass slots
+};
+
+// FP32 copy of a node box for pre-tests: lo.w = interaction radius x Rkern.
+struct __align__(16) NodeBoxF {
+    float4 lo;
+    float4 hi;
 };
 
 // Live per-stage timing with CUDA events on the launching stream (off by default).
@@ -88,7 +95,7 @@ struct Ctx {
     int key_bits = 32;
     u32 n_obj = 0, morton_count = 0, leaf_count = 0;
     DevBuf keys, sort_index, flags_a, flags_b, offsets, reduc, reduced;
-    DevBuf lchild, rchild, lflag, rflag, endrange, parent, boxes, visit;
+    DevBuf lchild, rchild, lflag, rflag, endrange, parent, boxes, visit, fboxes;
     bool has_rint = false;
 
     // ---- rank-ordered copies of merged fields
@@ -151,7 +158,10 @@ cudaError_t sync_scalars(Ctx &c);            // copy Scalars to pinned host, wai
 
 // neigh.cu
 cudaError_t build_rows(Ctx &c, u32 n_local);
-cudaError_t neigh_cache_build(Ctx &c, f64 h_tolerance);
+// pA/pB: optional FP32 hi/lo staging (A.xyz, B.xyz) with B.w = fl32(thr) of each rank;
+// when given, candidate pairs are pre-tested in FP32 (same resulting cache).
+cudaError_t neigh_cache_build(Ctx &c, f64 h_tolerance, const float4 *pA = nullptr,
+                              const float4 *pB = nullptr);
 cudaError_t tree_query(Ctx &c, const f64 *qx, const f64 *qy, const f64 *qz, u32 nq, int mode,
                        f64 s, u32 *counts, u32 *offsets, u32 *out, bool fill);
 

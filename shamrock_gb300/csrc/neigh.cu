@@ -17,7 +17,8 @@ namespace gbsph {
 
 namespace {
 
-constexpr int kStack = 64;
+constexpr int kStack   = 64;
+constexpr u32 kLeafCap = 256; // stage-1 slots per leaf in the one-pass build
 
 __device__ __forceinline__ void load_box(const NodeBox *__restrict__ b, f64 lo[3], f64 hi[3],
                                          f64 &rint) {
@@ -117,6 +118,67 @@ __global__ void k_leaf_fill(TreeView t, const u32 *__restrict__ off, u32 *__rest
     dfs(t, crit, [&](u32 leaf) { ent[w++] = leaf; });
 }
 
+// ---- stage 1, one pass into kLeafCap slots per leaf, optional FP32 pre-test.
+// For boxes a (the leaf) and n (a node) the criterion is
+//   C1 || C2,  C1 = a overlaps n grown by r_n,  C2 = a grown by r_a overlaps n,
+// which in exact arithmetic is  max_axis s <= max(r_n, r_a)  with the per-axis
+// separation s = max(n.lo - a.hi, a.lo - n.hi).  The FP32 estimate of s carries at most
+// ~2e-7 of the largest coordinate M plus 1e-7 relative; outside a band of
+// 1e-6 (M + R) the FP32 answer is certain, inside it the FP64 criterion decides.
+__global__ void k_boxes_f32(const NodeBox *__restrict__ b, u32 T, NodeBoxF *__restrict__ f) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T) return;
+    NodeBox v = b[i];
+    f[i].lo = make_float4(__double2float_rn(v.lo[0]), __double2float_rn(v.lo[1]),
+                          __double2float_rn(v.lo[2]), __double2float_rn(__dmul_rn(v.rint, kRkern)));
+    f[i].hi = make_float4(__double2float_rn(v.hi[0]), __double2float_rn(v.hi[1]),
+                          __double2float_rn(v.hi[2]), 0.f);
+}
+
+__global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *__restrict__ fb,
+                                                    u32 *__restrict__ cnt, u32 *__restrict__ off,
+                                                    u32 *__restrict__ ent, u32 *__restrict__ flags) {
+    u32 l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= t.L) return;
+    LeafCrit crit(t, l);
+    u32 c = 0, base = l * kLeafCap;
+    bool ok;
+    if (fb) {
+        float4 alo = __ldg(&fb[t.off() + l].lo), ahi = __ldg(&fb[t.off() + l].hi);
+        float4 rlo = __ldg(&fb[0].lo), rhi = __ldg(&fb[0].hi);
+        float M = fmaxf(fmaxf(fmaxf(fabsf(rlo.x), fabsf(rlo.y)), fmaxf(fabsf(rlo.z), fabsf(rhi.x))),
+                        fmaxf(fabsf(rhi.y), fabsf(rhi.z)));
+        float band_abs = 1e-6f * M;
+        ok = dfs(
+            t,
+            [&](u32 node) {
+                float4 nlo = __ldg(&fb[node].lo), nhi = __ldg(&fb[node].hi);
+                float sx = fmaxf(nlo.x - ahi.x, alo.x - nhi.x);
+                float sy = fmaxf(nlo.y - ahi.y, alo.y - nhi.y);
+                float sz = fmaxf(nlo.z - ahi.z, alo.z - nhi.z);
+                float sm = fmaxf(fmaxf(sx, sy), sz);
+                float R  = fmaxf(nlo.w, alo.w);
+                float band = band_abs + 1e-6f * R;
+                if (sm < R - band) return true;
+                if (sm > R + band) return false;
+                return crit(node);
+            },
+            [&](u32 leaf) {
+                if (c < kLeafCap) ent[base + c] = leaf;
+                c++;
+            });
+    } else {
+        ok = dfs(t, crit, [&](u32 leaf) {
+            if (c < kLeafCap) ent[base + c] = leaf;
+            c++;
+        });
+    }
+    if (!ok) atomicOr(flags, kFlagStackOverflow);
+    if (c > kLeafCap) atomicOr(flags, kFlagLeafCap);
+    cnt[l] = c;
+    off[l] = base;
+}
+
 // ---- rows: local particles in rank order
 __global__ void k_row_flags(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
                             u8 *__restrict__ flags) {
@@ -208,6 +270,61 @@ __global__ void __launch_bounds__(256) k_part_cache(
     if (!FILL) cnt[row] = c;
 }
 
+// ---- stage 2 with an FP32 pre-test (mixed precision).  The pair test is
+// r^2 <= max(thr_a, thr_b), thr = ((h htol)^2) R^2 in FP64.  r^2 is estimated in FP32
+// from hi/lo-split positions (relative error below ~3e-7) and compared with the FP32
+// rounding of max(thr_a, thr_b); outside a +-1e-5 relative band the answer is certain,
+// inside it the exact FP64 test of k_part_cache decides.  The cache is therefore
+// identical to the FP64 one.
+template<bool FILL>
+__global__ void __launch_bounds__(256) k_part_cache_f32(
+    const u32 *__restrict__ row_rank, u32 n_rows, const u32 *__restrict__ owner,
+    const u32 *__restrict__ leaf_cnt, const u32 *__restrict__ leaf_off,
+    const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const float4 *__restrict__ A,
+    const float4 *__restrict__ B, const f64 *__restrict__ sx, const f64 *__restrict__ sy,
+    const f64 *__restrict__ sz, const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ cnt,
+    const u32 *__restrict__ off, u32 *__restrict__ ent) {
+    u32 row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    u32 ra    = row_rank[row];
+    float4 Aa = __ldg(&A[ra]), Ba = __ldg(&B[ra]);
+    u32 leaf  = owner[row];
+    u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
+    u32 c = 0, w = FILL ? off[row] : 0;
+    const float lo_f = 1.f - 1e-5f, hi_f = 1.f + 1e-5f;
+    for (u32 k = k0; k < k1; k++) {
+        u32 lb = leaf_ent[k];
+        u32 r0 = reduc[lb], r1 = reduc[lb + 1];
+        for (u32 rb = r0; rb < r1; rb++) {
+            float4 Ab = __ldg(&A[rb]), Bb = __ldg(&B[rb]);
+            float dx = __fadd_rn(__fsub_rn(Aa.x, Ab.x), __fsub_rn(Ba.x, Bb.x));
+            float dy = __fadd_rn(__fsub_rn(Aa.y, Ab.y), __fsub_rn(Ba.y, Bb.y));
+            float dz = __fadd_rn(__fsub_rn(Aa.z, Ab.z), __fsub_rn(Ba.z, Bb.z));
+            float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            float tm = fmaxf(Ba.w, Bb.w);
+            bool in;
+            if (r2 < tm * lo_f) {
+                in = true;
+            } else if (r2 > tm * hi_f) {
+                in = false;
+            } else {
+                f64 rint_a = __dmul_rn(sh[ra], h_tol), rint_b = __dmul_rn(sh[rb], h_tol);
+                f64 thr_a  = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
+                f64 thr_b  = __dmul_rn(__dmul_rn(rint_b, rint_b), kRkern * kRkern);
+                f64 ex = __dsub_rn(sx[ra], sx[rb]), ey = __dsub_rn(sy[ra], sy[rb]),
+                    ez = __dsub_rn(sz[ra], sz[rb]);
+                f64 rab2 = dot3_rn(ex, ey, ez);
+                in       = !(rab2 > thr_a && rab2 > thr_b);
+            }
+            if (in) {
+                if (FILL) ent[w++] = rb;
+                c++;
+            }
+        }
+    }
+    if (!FILL) cnt[row] = c;
+}
+
 // ---- generic object query (CLBVHObjectIterator::rtree_for, CLBVHObjectIterator.hpp:127-169)
 template<bool FILL>
 __global__ void k_query(TreeView t, const f64 *__restrict__ qx, const f64 *__restrict__ qy,
@@ -277,7 +394,7 @@ cudaError_t build_rows(Ctx &c, u32 n_local) {
     return cudaGetLastError();
 }
 
-cudaError_t neigh_cache_build(Ctx &c, f64 h_tol) {
+cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *pA, const float4 *pB) {
     cudaStream_t s = c.stream;
     cudaError_t e;
     u32 L = c.leaf_count, n = c.n_local;
@@ -285,12 +402,20 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol) {
     Scalars *dsc = c.d_scalars.as<Scalars>();
     if ((e = c.leaf_cnt.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
     if ((e = c.leaf_off.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+    // Stage 1 in one pass into kLeafCap slots per leaf; a leaf with more candidates
+    // raises kFlagLeafCap and the two-pass exact build below runs instead.
+    if ((e = cudaMemsetAsync(&dsc->flags, 0, sizeof(u32), s)) != cudaSuccess) return e;
+    if ((e = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * kLeafCap + 1), s)) != cudaSuccess) return e;
+    const NodeBoxF *fb = nullptr;
+    if (pA) {
+        u32 T = 2 * L - 1;
+        if ((e = c.fboxes.ensure(sizeof(NodeBoxF) * (size_t) T, s)) != cudaSuccess) return e;
+        { k_boxes_f32<<<div_up(T, 256), 256, 0, s>>>(c.boxes.as<NodeBox>(), T, c.fboxes.as<NodeBoxF>()); GBSPH_COUNTED; }
+        fb = c.fboxes.as<NodeBoxF>();
+    }
     {
         ProfScope ps(c, kProfStage1, L);
-        { k_leaf_count<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_cnt.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
-        if ((e = scan_exclusive_u32(c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), L, &dsc->total,
-                                    c.scan_scratch, s)) != cudaSuccess)
-            return e;
+        { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
     }
     if ((e = c.owner.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
     if (n) {
@@ -300,14 +425,21 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol) {
                                                &dsc->flags); GBSPH_COUNTED; }
     }
     if ((e = sync_scalars(c)) != cudaSuccess) return e;
-    c.leaf_csr_total = c.h_scalars->total;
     if (c.h_scalars->flags & (kFlagStackOverflow | kFlagOwnerMissing)) {
         c.err = "neighbour cache: tree traversal failed (stack overflow or particle outside every leaf box)";
         return cudaErrorUnknown;
     }
-    if ((e = c.leaf_ent.ensure(sizeof(u32) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
-    {
+    c.leaf_csr_total = 0;
+    if (c.h_scalars->flags & kFlagLeafCap) {
+        // some leaf has more than kLeafCap candidate leaves: exact two-pass build
         ProfScope ps(c, kProfStage1, 0);
+        { k_leaf_count<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_cnt.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
+        if ((e = scan_exclusive_u32(c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), L, &dsc->total,
+                                    c.scan_scratch, s)) != cudaSuccess)
+            return e;
+        if ((e = sync_scalars(c)) != cudaSuccess) return e;
+        c.leaf_csr_total = c.h_scalars->total;
+        if ((e = c.leaf_ent.ensure(sizeof(u32) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
         { k_leaf_fill<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_off.as<u32>(), c.leaf_ent.as<u32>()); GBSPH_COUNTED; }
     }
 
@@ -315,10 +447,18 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol) {
     if ((e = c.csr_off.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
     if (n) {
         ProfScope ps(c, kProfCacheCount, n);
+        if (pA) {
+            { k_part_cache_f32<false><<<div_up(n, 256), 256, 0, s>>>(
+                c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
+                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), pA, pB,
+                c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol,
+                c.csr_cnt.as<u32>(), nullptr, nullptr); GBSPH_COUNTED; }
+        } else {
         { k_part_cache<false><<<div_up(n, 256), 256, 0, s>>>(
             c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
             c.leaf_ent.as<u32>(), c.reduc.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
             c.sh.as<f64>(), h_tol, c.csr_cnt.as<u32>(), nullptr, nullptr); GBSPH_COUNTED; }
+        }
     }
     if ((e = scan_exclusive_u32(c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), n, &dsc->total,
                                 c.scan_scratch, s)) != cudaSuccess)
@@ -328,10 +468,18 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol) {
     if ((e = c.csr_ent.ensure(sizeof(u32) * (c.csr_total + 1), s)) != cudaSuccess) return e;
     if (n) {
         ProfScope ps(c, kProfCacheFill, c.csr_total);
+        if (pA) {
+            { k_part_cache_f32<true><<<div_up(n, 256), 256, 0, s>>>(
+                c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
+                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), pA, pB,
+                c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, nullptr,
+                c.csr_off.as<u32>(), c.csr_ent.as<u32>()); GBSPH_COUNTED; }
+        } else {
         { k_part_cache<true><<<div_up(n, 256), 256, 0, s>>>(
             c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
             c.leaf_ent.as<u32>(), c.reduc.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
             c.sh.as<f64>(), h_tol, nullptr, c.csr_off.as<u32>(), c.csr_ent.as<u32>()); GBSPH_COUNTED; }
+        }
     }
     c.cache_valid = true;
     return cudaGetLastError();

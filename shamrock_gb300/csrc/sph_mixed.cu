@@ -35,14 +35,19 @@ __device__ __forceinline__ f64 rho_h64(f64 m, f64 h) {
     return m * (kHfact / h) * (kHfact / h) * (kHfact / h);
 }
 
+// B.w carries fl32 of the neighbour-cache threshold ((h htol)^2) R^2 (computed in FP64
+// in the reference's order) for the FP32 pre-test of the cache build; the corrector
+// staging later overwrites it with c_s.
 __global__ void k_stage_pos(u32 N, const f64 *__restrict__ sx, const f64 *__restrict__ sy,
-                            const f64 *__restrict__ sz, const f64 *__restrict__ sh,
+                            const f64 *__restrict__ sz, const f64 *__restrict__ sh, f64 h_tol,
                             float4 *__restrict__ A, float4 *__restrict__ B) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
     f64 x = sx[r], y = sy[r], z = sz[r];
+    f64 rint = __dmul_rn(sh[r], h_tol);
+    f64 thr  = __dmul_rn(__dmul_rn(rint, rint), kRkern * kRkern);
     A[r] = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / sh[r]));
-    B[r] = make_float4(lo32(x), lo32(y), lo32(z), 0.f);
+    B[r] = make_float4(lo32(x), lo32(y), lo32(z), __double2float_rn(thr));
 }
 
 // hydro staging from FP64 fields in the entry index space
@@ -296,13 +301,13 @@ cudaError_t ensure_mixed(Ctx &c, u32 N) {
 
 } // namespace
 
-cudaError_t stage_positions_mixed(Ctx &c, u32 N) {
+cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol) {
     cudaError_t e = ensure_mixed(c, N);
     if (e != cudaSuccess) return e;
     MixedSpace ms = mixed_space(c, N);
     ProfScope ps(c, kProfTree, N);
     { k_stage_pos<<<div_up(N, 256), 256, 0, c.stream>>>(N, c.sx.as<f64>(), c.sy.as<f64>(),
-                                                      c.sz.as<f64>(), c.sh.as<f64>(),
+                                                      c.sz.as<f64>(), c.sh.as<f64>(), h_tol,
                                                       (float4 *) ms.A, (float4 *) ms.B); GBSPH_COUNTED; }
     return cudaGetLastError();
 }

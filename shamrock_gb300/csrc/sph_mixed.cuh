@@ -17,7 +17,7 @@ struct MixedSpace {
     const float4 *A, *B, *C, *D, *E;
 };
 
-cudaError_t stage_positions_mixed(Ctx &c, u32 N);
+cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol);
 cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
                             f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters);
 cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);

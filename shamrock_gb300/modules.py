@@ -120,9 +120,11 @@ class Tree:
         return counts.cpu().numpy().view(np.uint32), out[:tot.value].cpu().numpy().view(np.uint32)
 
 
-def neighbour_cache(ctx, n_local, htol):
-    """Two-stage cache over the last tree; returns the reference-layout CSR on the GPU."""
-    ctx.call("gbsph_neighbour_cache", n_local, htol, None)
+def neighbour_cache(ctx, n_local, htol, precision="fp64"):
+    """Two-stage cache over the last tree; returns the reference-layout CSR on the GPU.
+    precision "mixed" pre-tests pairs in FP32 (the resulting cache is the same)."""
+    ctx.call("gbsph_neighbour_cache", n_local, htol,
+             L.GBSPH_MIXED if precision == "mixed" else L.GBSPH_FP64, None)
     tot, ltot = C.c_uint64(), C.c_uint64()
     ctx.call("gbsph_cache_size", C.byref(tot), C.byref(ltot))
     cnt = torch.empty(n_local, dtype=torch.int32, device="cuda")

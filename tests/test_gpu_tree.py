@@ -153,8 +153,11 @@ def test_periodic_ghosts_vs_oracle(gctx, M, n_cells, jitter):
     assert np.array_equal(g["merged_h"][n:], s["h"][src])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("n_cells,jitter,level", [(6, 0.0, 3), (8, 0.05, 3), (10, 0.2, 1), (12, 0.05, 3)])
-def test_neighbour_cache_vs_oracle(gctx, M, n_cells, jitter, level):
+def test_neighbour_cache_vs_oracle(gctx, M, n_cells, jitter, level, precision):
+    """Bit-exact CSR; the mixed build pre-tests pairs in FP32 and must give the same cache
+    (the unjittered lattice puts many pairs exactly on the threshold)."""
     s = _lattice(n_cells, jitter, 5)
     n = len(s["h"])
     g = M.periodic_ghosts(gctx, s["pos"], s["h"], [0, 0, 0], [1, 1, 1], 1.1)
@@ -162,7 +165,7 @@ def test_neighbour_cache_vs_oracle(gctx, M, n_cells, jitter, level):
     lo = np.nextafter(mpos.min(0), -np.inf)
     hi = np.nextafter(mpos.max(0), np.inf)
     t = M.Tree(gctx, mpos, lo, hi, level, h=mh, htol=1.1)
-    csr = M.neighbour_cache(gctx, n, 1.1)
+    csr = M.neighbour_cache(gctx, n, 1.1, precision)
     o = O.Tree(mpos, lo, hi, level, h=mh, htol=1.1)
     oc = o.neigh_cache(mpos, mh, n, 1.1)
     assert np.array_equal(csr["cnt"].cpu().numpy().view(np.uint32), oc["cnt"])
