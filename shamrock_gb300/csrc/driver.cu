@@ -332,8 +332,7 @@ int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, uint32_
     CU(build_rows(c, n_local));
     if (precision == GBSPH_MIXED) {
         CU(stage_positions_mixed(c, c.n_obj, htol));
-        const float4 *fA = c.f_pos.as<float4>();
-        CU(neigh_cache_build(c, htol, fA, fA + c.n_obj));
+        CU(neigh_cache_build(c, htol, mixed_positions(c)));
     } else {
         CU(neigh_cache_build(c, htol));
     }
@@ -514,8 +513,7 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
         CU(build_rows(c, n));
         if (mixed) {
             CU(stage_positions_mixed(c, N, cfg->htol_up_coarse));
-            const float4 *fA = c.f_pos.as<float4>();
-            CU(neigh_cache_build(c, cfg->htol_up_coarse, fA, fA + N));
+            CU(neigh_cache_build(c, cfg->htol_up_coarse, mixed_positions(c)));
         } else {
             CU(neigh_cache_build(c, cfg->htol_up_coarse));
         }

@@ -28,6 +28,7 @@ struct Scalars {
     u64 epsv2_max;     // ordered-u64 max of |dv corrector|^2
     u64 dt_min;        // ordered-u64 min of per-particle CFL dt
     u64 n_unconverged; // particles whose per-thread iteration cap was hit
+    u64 csr_entries;   // stage-2 entries of the one-pass cache build
     f64 sum_v2;        // sum of |v|^2 after the corrector
     f64 cons[8];       // conservation totals (momentum, energies)
     u32 total;         // scan totals
@@ -42,7 +43,8 @@ enum KernelFlags : u32 {
     kFlagStackOverflow = 1u,
     kFlagOwnerMissing  = 2u,
     kFlagCsrOverflow   = 4u,
-    kFlagLeafCap       = 8u, // a leaf had more stage-1 candidates than the one-pass slots
+    kFlagLeafCap       = 8u,  // a leaf had more stage-1 candidates than the one-pass slots
+    kFlagCsrCap        = 16u, // a row had more stage-2 entries than the one-pass slots
 };
 
 // FP32 copy of a node box for pre-tests: lo.w = interaction radius x Rkern.
@@ -158,10 +160,9 @@ cudaError_t sync_scalars(Ctx &c);            // copy Scalars to pinned host, wai
 
 // neigh.cu
 cudaError_t build_rows(Ctx &c, u32 n_local);
-// pA/pB: optional FP32 hi/lo staging (A.xyz, B.xyz) with B.w = fl32(thr) of each rank;
+// P: optional FP32 position records (2 float4 per rank: hi + 1/h, lo + fl32(thr));
 // when given, candidate pairs are pre-tested in FP32 (same resulting cache).
-cudaError_t neigh_cache_build(Ctx &c, f64 h_tolerance, const float4 *pA = nullptr,
-                              const float4 *pB = nullptr);
+cudaError_t neigh_cache_build(Ctx &c, f64 h_tolerance, const float4 *P = nullptr);
 cudaError_t tree_query(Ctx &c, const f64 *qx, const f64 *qy, const f64 *qz, u32 nq, int mode,
                        f64 s, u32 *counts, u32 *offsets, u32 *out, bool fill);
 

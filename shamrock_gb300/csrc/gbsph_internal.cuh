@@ -105,6 +105,9 @@ struct OpAddF64 {
 struct OpAddU32 {
     __device__ u32 operator()(u32 a, u32 b) const { return a + b; }
 };
+struct OpAddU64 {
+    __device__ u64 operator()(u64 a, u64 b) const { return a + b; }
+};
 
 inline u32 div_up(u64 a, u64 b) { return (u32) ((a + b - 1) / b); }
 

@@ -13,12 +13,15 @@
 
 #include "gbsph_ctx.cuh"
 
+#include <type_traits>
+
 namespace gbsph {
 
 namespace {
 
 constexpr int kStack   = 64;
 constexpr u32 kLeafCap = 256; // stage-1 slots per leaf in the one-pass build
+constexpr u32 kRowCap  = 192; // stage-2 slots per row in the one-pass build (multiple of 4)
 
 __device__ __forceinline__ void load_box(const NodeBox *__restrict__ b, f64 lo[3], f64 hi[3],
                                          f64 &rint) {
@@ -236,93 +239,83 @@ __global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows
 }
 
 // ---- stage 2 (NeighbourCache.cpp:492-591)
-template<bool FILL>
+// MODE kCount: per-row count; kFill: entries at off[row] (compact CSR after a scan);
+// kOnePass: entries straight into kRowCap slots per row (off[row] = row * kRowCap),
+// flagging kFlagCsrCap when a row overflows so the host reruns the two-pass build.
+//
+// F32: the pair test is r^2 <= max(thr_a, thr_b), thr = ((h htol)^2) R^2 in FP64.  r^2
+// is estimated in FP32 from hi/lo-split positions (relative error below ~3e-7) and
+// compared with the FP32 rounding of max(thr_a, thr_b) carried in the position record;
+// outside a +-1e-5 relative band the answer is certain, inside it the exact FP64 test
+// decides.  The cache is therefore identical to the FP64 one.
+enum CacheMode { kCount = 0, kFill = 1, kOnePass = 2 };
+
+template<int MODE, bool F32>
 __global__ void __launch_bounds__(256) k_part_cache(
     const u32 *__restrict__ row_rank, u32 n_rows, const u32 *__restrict__ owner,
     const u32 *__restrict__ leaf_cnt, const u32 *__restrict__ leaf_off,
-    const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const f64 *__restrict__ sx,
-    const f64 *__restrict__ sy, const f64 *__restrict__ sz, const f64 *__restrict__ sh,
-    f64 h_tol, u32 *__restrict__ cnt, const u32 *__restrict__ off, u32 *__restrict__ ent) {
+    const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const float4 *__restrict__ P,
+    const f64 *__restrict__ sx, const f64 *__restrict__ sy, const f64 *__restrict__ sz,
+    const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ cnt, u32 *__restrict__ off,
+    u32 *__restrict__ ent, Scalars *sc) {
     u32 row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= n_rows) return;
-    u32 ra    = row_rank[row];
-    f64 xa    = sx[ra], ya = sy[ra], za = sz[ra];
-    f64 rint_a = __dmul_rn(sh[ra], h_tol);
-    f64 thr_a = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
-    u32 leaf  = owner[row];
-    u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
-    u32 c = 0, w = FILL ? off[row] : 0;
-    for (u32 k = k0; k < k1; k++) {
-        u32 lb = leaf_ent[k];
-        u32 r0 = reduc[lb], r1 = reduc[lb + 1];
-        for (u32 rb = r0; rb < r1; rb++) {
-            f64 dx = __dsub_rn(xa, sx[rb]), dy = __dsub_rn(ya, sy[rb]), dz = __dsub_rn(za, sz[rb]);
-            f64 rab2   = dot3_rn(dx, dy, dz);
-            f64 rint_b = __dmul_rn(sh[rb], h_tol);
-            f64 thr_b  = __dmul_rn(__dmul_rn(rint_b, rint_b), kRkern * kRkern);
-            bool no_interact = rab2 > thr_a && rab2 > thr_b;
-            if (!no_interact) {
-                if (FILL) ent[w++] = rb;
-                c++;
+    u32 c   = 0;
+    if (row < n_rows) {
+        u32 ra     = row_rank[row];
+        f64 xa     = sx[ra], ya = sy[ra], za = sz[ra];
+        f64 rint_a = __dmul_rn(sh[ra], h_tol);
+        f64 thr_a  = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
+        float4 Aa = make_float4(0, 0, 0, 0), Ba = Aa;
+        if (F32) {
+            Aa = __ldg(&P[2 * (size_t) ra]);
+            Ba = __ldg(&P[2 * (size_t) ra + 1]);
+        }
+        const float lo_f = 1.f - 1e-5f, hi_f = 1.f + 1e-5f;
+        u32 leaf = owner[row];
+        u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
+        u32 w = (MODE == kFill) ? off[row] : ((MODE == kOnePass) ? row * kRowCap : 0);
+        for (u32 k = k0; k < k1; k++) {
+            u32 lb = leaf_ent[k];
+            u32 r0 = reduc[lb], r1 = reduc[lb + 1];
+            for (u32 rb = r0; rb < r1; rb++) {
+                int decided = -1;
+                if (F32) {
+                    float4 Ab = __ldg(&P[2 * (size_t) rb]), Bb = __ldg(&P[2 * (size_t) rb + 1]);
+                    float dx = __fadd_rn(__fsub_rn(Aa.x, Ab.x), __fsub_rn(Ba.x, Bb.x));
+                    float dy = __fadd_rn(__fsub_rn(Aa.y, Ab.y), __fsub_rn(Ba.y, Bb.y));
+                    float dz = __fadd_rn(__fsub_rn(Aa.z, Ab.z), __fsub_rn(Ba.z, Bb.z));
+                    float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    float tm = fmaxf(Ba.w, Bb.w);
+                    decided  = (r2 < tm * lo_f) ? 1 : ((r2 > tm * hi_f) ? 0 : -1);
+                }
+                bool in;
+                if (decided >= 0) {
+                    in = decided == 1;
+                } else {
+                    f64 dx = __dsub_rn(xa, sx[rb]), dy = __dsub_rn(ya, sy[rb]),
+                        dz = __dsub_rn(za, sz[rb]);
+                    f64 rab2   = dot3_rn(dx, dy, dz);
+                    f64 rint_b = __dmul_rn(sh[rb], h_tol);
+                    f64 thr_b  = __dmul_rn(__dmul_rn(rint_b, rint_b), kRkern * kRkern);
+                    in = !(rab2 > thr_a && rab2 > thr_b);
+                }
+                if (in) {
+                    if (MODE == kFill) ent[w + c] = rb;
+                    if (MODE == kOnePass && c < kRowCap) ent[w + c] = rb;
+                    c++;
+                }
             }
         }
-    }
-    if (!FILL) cnt[row] = c;
-}
-
-// ---- stage 2 with an FP32 pre-test (mixed precision).  The pair test is
-// r^2 <= max(thr_a, thr_b), thr = ((h htol)^2) R^2 in FP64.  r^2 is estimated in FP32
-// from hi/lo-split positions (relative error below ~3e-7) and compared with the FP32
-// rounding of max(thr_a, thr_b); outside a +-1e-5 relative band the answer is certain,
-// inside it the exact FP64 test of k_part_cache decides.  The cache is therefore
-// identical to the FP64 one.
-template<bool FILL>
-__global__ void __launch_bounds__(256) k_part_cache_f32(
-    const u32 *__restrict__ row_rank, u32 n_rows, const u32 *__restrict__ owner,
-    const u32 *__restrict__ leaf_cnt, const u32 *__restrict__ leaf_off,
-    const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const float4 *__restrict__ A,
-    const float4 *__restrict__ B, const f64 *__restrict__ sx, const f64 *__restrict__ sy,
-    const f64 *__restrict__ sz, const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ cnt,
-    const u32 *__restrict__ off, u32 *__restrict__ ent) {
-    u32 row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= n_rows) return;
-    u32 ra    = row_rank[row];
-    float4 Aa = __ldg(&A[ra]), Ba = __ldg(&B[ra]);
-    u32 leaf  = owner[row];
-    u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
-    u32 c = 0, w = FILL ? off[row] : 0;
-    const float lo_f = 1.f - 1e-5f, hi_f = 1.f + 1e-5f;
-    for (u32 k = k0; k < k1; k++) {
-        u32 lb = leaf_ent[k];
-        u32 r0 = reduc[lb], r1 = reduc[lb + 1];
-        for (u32 rb = r0; rb < r1; rb++) {
-            float4 Ab = __ldg(&A[rb]), Bb = __ldg(&B[rb]);
-            float dx = __fadd_rn(__fsub_rn(Aa.x, Ab.x), __fsub_rn(Ba.x, Bb.x));
-            float dy = __fadd_rn(__fsub_rn(Aa.y, Ab.y), __fsub_rn(Ba.y, Bb.y));
-            float dz = __fadd_rn(__fsub_rn(Aa.z, Ab.z), __fsub_rn(Ba.z, Bb.z));
-            float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            float tm = fmaxf(Ba.w, Bb.w);
-            bool in;
-            if (r2 < tm * lo_f) {
-                in = true;
-            } else if (r2 > tm * hi_f) {
-                in = false;
-            } else {
-                f64 rint_a = __dmul_rn(sh[ra], h_tol), rint_b = __dmul_rn(sh[rb], h_tol);
-                f64 thr_a  = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
-                f64 thr_b  = __dmul_rn(__dmul_rn(rint_b, rint_b), kRkern * kRkern);
-                f64 ex = __dsub_rn(sx[ra], sx[rb]), ey = __dsub_rn(sy[ra], sy[rb]),
-                    ez = __dsub_rn(sz[ra], sz[rb]);
-                f64 rab2 = dot3_rn(ex, ey, ez);
-                in       = !(rab2 > thr_a && rab2 > thr_b);
-            }
-            if (in) {
-                if (FILL) ent[w++] = rb;
-                c++;
-            }
+        if (MODE != kFill) cnt[row] = c;
+        if (MODE == kOnePass) {
+            off[row] = w;
+            if (c > kRowCap) atomicOr(&sc->flags, kFlagCsrCap);
         }
     }
-    if (!FILL) cnt[row] = c;
+    if (MODE == kOnePass) {
+        u64 tot = block_reduce((u64) c, OpAddU64{}, 0ull);
+        if (threadIdx.x == 0) atomicAdd((unsigned long long *) &sc->csr_entries, (unsigned long long) tot);
+    }
 }
 
 // ---- generic object query (CLBVHObjectIterator::rtree_for, CLBVHObjectIterator.hpp:127-169)
@@ -394,7 +387,7 @@ cudaError_t build_rows(Ctx &c, u32 n_local) {
     return cudaGetLastError();
 }
 
-cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *pA, const float4 *pB) {
+cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     cudaStream_t s = c.stream;
     cudaError_t e;
     u32 L = c.leaf_count, n = c.n_local;
@@ -407,7 +400,7 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *pA, const float4 
     if ((e = cudaMemsetAsync(&dsc->flags, 0, sizeof(u32), s)) != cudaSuccess) return e;
     if ((e = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * kLeafCap + 1), s)) != cudaSuccess) return e;
     const NodeBoxF *fb = nullptr;
-    if (pA) {
+    if (P) {
         u32 T = 2 * L - 1;
         if ((e = c.fboxes.ensure(sizeof(NodeBoxF) * (size_t) T, s)) != cudaSuccess) return e;
         { k_boxes_f32<<<div_up(T, 256), 256, 0, s>>>(c.boxes.as<NodeBox>(), T, c.fboxes.as<NodeBoxF>()); GBSPH_COUNTED; }
@@ -445,41 +438,50 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *pA, const float4 
 
     if ((e = c.csr_cnt.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
     if ((e = c.csr_off.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
-    if (n) {
-        ProfScope ps(c, kProfCacheCount, n);
-        if (pA) {
-            { k_part_cache_f32<false><<<div_up(n, 256), 256, 0, s>>>(
+    // the padded one-pass layout needs row * kRowCap to fit the u32 offsets
+    const bool one_pass = (u64) n * kRowCap < 0xffffffffull;
+    if (one_pass)
+        if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * kRowCap + 1), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(&dsc->csr_entries, 0, sizeof(u64), s)) != cudaSuccess) return e;
+    // launch helper for the stage-2 kernel family
+    auto part = [&](auto mode_tag, u32 *cnt, u32 *off, u32 *ent) {
+        constexpr int MODE = decltype(mode_tag)::value;
+        if (P) {
+            { k_part_cache<MODE, true><<<div_up(n, 256), 256, 0, s>>>(
                 c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
-                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), pA, pB,
-                c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol,
-                c.csr_cnt.as<u32>(), nullptr, nullptr); GBSPH_COUNTED; }
+                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), P, c.sx.as<f64>(),
+                c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off, ent, dsc); GBSPH_COUNTED; }
         } else {
-        { k_part_cache<false><<<div_up(n, 256), 256, 0, s>>>(
-            c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
-            c.leaf_ent.as<u32>(), c.reduc.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
-            c.sh.as<f64>(), h_tol, c.csr_cnt.as<u32>(), nullptr, nullptr); GBSPH_COUNTED; }
+            { k_part_cache<MODE, false><<<div_up(n, 256), 256, 0, s>>>(
+                c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
+                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), nullptr,
+                c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off,
+                ent, dsc); GBSPH_COUNTED; }
         }
+    };
+    using OnePass = std::integral_constant<int, kOnePass>;
+    using Count   = std::integral_constant<int, kCount>;
+    using Fill    = std::integral_constant<int, kFill>;
+    if (n && one_pass) {
+        ProfScope ps(c, kProfCacheFill, n);
+        part(OnePass{}, c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>());
     }
-    if ((e = scan_exclusive_u32(c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), n, &dsc->total,
-                                c.scan_scratch, s)) != cudaSuccess)
-        return e;
     if ((e = sync_scalars(c)) != cudaSuccess) return e;
-    c.csr_total = c.h_scalars->total;
-    if ((e = c.csr_ent.ensure(sizeof(u32) * (c.csr_total + 1), s)) != cudaSuccess) return e;
-    if (n) {
-        ProfScope ps(c, kProfCacheFill, c.csr_total);
-        if (pA) {
-            { k_part_cache_f32<true><<<div_up(n, 256), 256, 0, s>>>(
-                c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
-                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), pA, pB,
-                c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, nullptr,
-                c.csr_off.as<u32>(), c.csr_ent.as<u32>()); GBSPH_COUNTED; }
-        } else {
-        { k_part_cache<true><<<div_up(n, 256), 256, 0, s>>>(
-            c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
-            c.leaf_ent.as<u32>(), c.reduc.as<u32>(), c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
-            c.sh.as<f64>(), h_tol, nullptr, c.csr_off.as<u32>(), c.csr_ent.as<u32>()); GBSPH_COUNTED; }
+    c.csr_total = c.h_scalars->csr_entries;
+    if (n && (!one_pass || (c.h_scalars->flags & kFlagCsrCap))) {
+        // a row has more than kRowCap entries: two-pass build into a compact CSR
+        {
+            ProfScope ps(c, kProfCacheCount, n);
+            part(Count{}, c.csr_cnt.as<u32>(), nullptr, nullptr);
         }
+        if ((e = scan_exclusive_u32(c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), n, &dsc->total,
+                                    c.scan_scratch, s)) != cudaSuccess)
+            return e;
+        if ((e = sync_scalars(c)) != cudaSuccess) return e;
+        c.csr_total = c.h_scalars->total;
+        if ((e = c.csr_ent.ensure(sizeof(u32) * (c.csr_total + 1), s)) != cudaSuccess) return e;
+        ProfScope ps(c, kProfCacheFill, 0);
+        part(Fill{}, nullptr, c.csr_off.as<u32>(), c.csr_ent.as<u32>());
     }
     c.cache_valid = true;
     return cudaGetLastError();

@@ -4,6 +4,9 @@
 // absolute positions, the Newton update and its convergence test (eps_h), the
 // leapfrog corrector and CFL, and the global totals.  Same physics and neighbour
 // set as the FP64 kernels (sph64.cu); see those for the reference citations.
+//
+// Neighbour loops take CSR entries four at a time and issue the four position-record
+// loads together, so several L2 round trips are in flight per thread.
 
 #include "sph_mixed.cuh"
 
@@ -40,63 +43,72 @@ __device__ __forceinline__ f64 rho_h64(f64 m, f64 h) {
 // staging later overwrites it with c_s.
 __global__ void k_stage_pos(u32 N, const f64 *__restrict__ sx, const f64 *__restrict__ sy,
                             const f64 *__restrict__ sz, const f64 *__restrict__ sh, f64 h_tol,
-                            float4 *__restrict__ A, float4 *__restrict__ B) {
+                            float4 *__restrict__ P) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
     f64 x = sx[r], y = sy[r], z = sz[r];
     f64 rint = __dmul_rn(sh[r], h_tol);
     f64 thr  = __dmul_rn(__dmul_rn(rint, rint), kRkern * kRkern);
-    A[r] = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / sh[r]));
-    B[r] = make_float4(lo32(x), lo32(y), lo32(z), __double2float_rn(thr));
+    P[2 * (size_t) r]     = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / sh[r]));
+    P[2 * (size_t) r + 1] = make_float4(lo32(x), lo32(y), lo32(z), __double2float_rn(thr));
 }
 
 // hydro staging from FP64 fields in the entry index space
 __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__restrict__ y,
                               const f64 *__restrict__ z, HydroSpace hs, f64 pmass,
-                              float4 *__restrict__ A, float4 *__restrict__ B,
-                              float4 *__restrict__ C, float4 *__restrict__ D,
-                              float4 *__restrict__ E) {
+                              float4 *__restrict__ P, float4 *__restrict__ H) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
-    f64 h = hs.h[r], om = hs.omega[r], P = hs.P[r];
+    f64 h = hs.h[r], om = hs.omega[r], Pr = hs.P[r];
     f64 rho = rho_h64(pmass, h);
     float hinv = __double2float_rn(1.0 / h);
+    size_t p2 = 2 * (size_t) r, h3 = 3 * (size_t) r;
     if (x) {
-        A[r] = make_float4(hi32(x[r]), hi32(y[r]), hi32(z[r]), hinv);
-        B[r] = make_float4(lo32(x[r]), lo32(y[r]), lo32(z[r]), __double2float_rn(hs.cs[r]));
+        P[p2]     = make_float4(hi32(x[r]), hi32(y[r]), hi32(z[r]), hinv);
+        P[p2 + 1] = make_float4(lo32(x[r]), lo32(y[r]), lo32(z[r]), __double2float_rn(hs.cs[r]));
     } else {
-        ((float *) &A[r])[3] = hinv;
-        ((float *) &B[r])[3] = __double2float_rn(hs.cs[r]);
+        ((float *) &P[p2])[3]     = hinv;
+        ((float *) &P[p2 + 1])[3] = __double2float_rn(hs.cs[r]);
     }
     f64 vx = hs.vx[r], vy = hs.vy[r], vz = hs.vz[r];
-    C[r] = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(hs.u[r]));
-    D[r] = make_float4(lo32(vx), lo32(vy), lo32(vz), __double2float_rn(rho));
+    H[h3]     = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(hs.u[r]));
+    H[h3 + 1] = make_float4(lo32(vx), lo32(vy), lo32(vz), __double2float_rn(rho));
     f64 sub = rho * rho * om;
     f64 c1  = (sub != 0 && sub == sub) ? 1. / sub : 0.;
-    E[r]    = make_float4(hi32(P), lo32(P), __double2float_rn(c1), __double2float_rn(1. / (rho * om)));
+    H[h3 + 2] = make_float4(hi32(Pr), lo32(Pr), __double2float_rn(c1), __double2float_rn(1. / (rho * om)));
 }
 
 // sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a
 __device__ __forceinline__ void density_sums_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
                                                  u32 k0, u32 k1, float hinv, float &sf, float &sg) {
-    float4 Aa = __ldg(&ms.A[a]), Ba = __ldg(&ms.B[a]);
+    float4 Aa = __ldg(&ms.P[2 * (size_t) a]), Ba = __ldg(&ms.P[2 * (size_t) a + 1]);
     float cf = 0.f, cg = 0.f;
     sf = 0.f;
     sg = 0.f;
     float hinv2 = hinv * hinv;
-    for (u32 k = k0; k < k1; k++) {
-        u32 b     = __ldg(&rs.ent[k]);
-        float4 Ab = __ldg(&ms.A[b]), Bb = __ldg(&ms.B[b]);
-        float dx = (Aa.x - Ab.x) + (Ba.x - Bb.x);
-        float dy = (Aa.y - Ab.y) + (Ba.y - Bb.y);
-        float dz = (Aa.z - Ab.z) + (Ba.z - Bb.z);
-        float q2 = (dx * dx + dy * dy + dz * dz) * hinv2;
-        if (q2 > 4.f) continue;
-        float q  = sqrtf(q2);
-        float f  = m4_f32(q);
-        float df = m4_df32(q);
-        kahan_add(sf, cf, f);
-        kahan_add(sg, cg, 3.f * f + q * df);
+    for (u32 k = k0; k < k1; k += 4) {
+        u32 bb[4];
+        float4 Ab[4], Bb[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) bb[j] = (k + j < k1) ? __ldg(&rs.ent[k + j]) : a;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            Ab[j] = __ldg(&ms.P[2 * (size_t) bb[j]]);
+            Bb[j] = __ldg(&ms.P[2 * (size_t) bb[j] + 1]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float dx = (Aa.x - Ab[j].x) + (Ba.x - Bb[j].x);
+            float dy = (Aa.y - Ab[j].y) + (Ba.y - Bb[j].y);
+            float dz = (Aa.z - Ab[j].z) + (Ba.z - Bb[j].z);
+            float q2 = (dx * dx + dy * dy + dz * dz) * hinv2;
+            if (k + j >= k1 || q2 > 4.f) continue;
+            float q  = sqrtf(q2);
+            float f  = m4_f32(q);
+            float df = m4_df32(q);
+            kahan_add(sf, cf, f);
+            kahan_add(sg, cg, 3.f * f + q * df);
+        }
     }
 }
 
@@ -172,11 +184,14 @@ struct MixedParams {
 //   F = sum (ca Fa + cb Fb) r_hat   (acceleration = -m F)
 //   U = sum [AVPa c1a Fa (v.r_hat) + 0.5 alpha_u vsig_u (u_a - u_b)(Fa c2a + Fb c2b)]
 //   (du/dt = m U), and the v_sig maximum of the reference's separate v_sig kernel.
+// Self and coincident pairs (r = 0) contribute nothing and are skipped, which also
+// makes padding a partial batch of four with the row's own index harmless.
 __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
                                                u32 k0, u32 k1, const MixedParams &p, float &Fx,
                                                float &Fy, float &Fz, float &U, float &vsig_max) {
-    float4 Aa = __ldg(&ms.A[a]), Ba = __ldg(&ms.B[a]), Ca = __ldg(&ms.C[a]),
-           Da = __ldg(&ms.D[a]), Ea = __ldg(&ms.E[a]);
+    float4 Aa = __ldg(&ms.P[2 * (size_t) a]), Ba = __ldg(&ms.P[2 * (size_t) a + 1]);
+    float4 Ca = __ldg(&ms.H[3 * (size_t) a]), Da = __ldg(&ms.H[3 * (size_t) a + 1]),
+           Ea = __ldg(&ms.H[3 * (size_t) a + 2]);
     const float hia = Aa.w, cs_a = Ba.w, u_a = Ca.w, rho_a = Da.w;
     const float P_a = Ea.x + Ea.y, c1a = Ea.z, c2a = Ea.w;
     const float k4a = hia * hia * hia * hia * kNorm3dF;
@@ -184,41 +199,52 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
     float cx = 0.f, cy = 0.f, cz = 0.f, cu = 0.f;
     Fx = Fy = Fz = U = 0.f;
     vsig_max = 0.f;
-    for (u32 k = k0; k < k1; k++) {
-        u32 b     = __ldg(&rs.ent[k]);
-        float4 Ab = __ldg(&ms.A[b]), Bb = __ldg(&ms.B[b]);
-        float dx = (Aa.x - Ab.x) + (Ba.x - Bb.x);
-        float dy = (Aa.y - Ab.y) + (Ba.y - Bb.y);
-        float dz = (Aa.z - Ab.z) + (Ba.z - Bb.z);
-        float r2 = dx * dx + dy * dy + dz * dz;
-        float hib = Ab.w;
-        if ((r2 * hia2 > 4.f && r2 * hib * hib > 4.f) || r2 == 0.f) continue;
-        float4 Cb = __ldg(&ms.C[b]), Db = __ldg(&ms.D[b]), Eb = __ldg(&ms.E[b]);
-        float rinv = rsqrtf(r2);
-        float rab  = r2 * rinv;
-        float Fa   = k4a * m4_df32(rab * hia);
-        float Fb   = hib * hib * hib * hib * kNorm3dF * m4_df32(rab * hib);
-        float rx = dx * rinv, ry = dy * rinv, rz = dz * rinv;
-        float vx = (Ca.x - Cb.x) + (Da.x - Db.x);
-        float vy = (Ca.y - Cb.y) + (Da.y - Db.y);
-        float vz = (Ca.z - Cb.z) + (Da.z - Db.z);
-        float vr  = vx * rx + vy * ry + vz * rz;
-        float avr = fabsf(vr);
-        float rho_b = Db.w, cs_b = Bb.w;
-        float vsig_a = p.alpha_AV * cs_a + p.beta_AV * avr;
-        float vsig_b = p.alpha_AV * cs_b + p.beta_AV * avr;
-        float dP     = (Ea.x - Eb.x) + (Ea.y - Eb.y);
-        float vsig_u = sqrtf(fabsf(dP) / ((rho_a + rho_b) * 0.5f));
-        float qa = fmaxf(-0.5f * rho_a * vsig_a * vr, 0.f);
-        float qb = fmaxf(-0.5f * rho_b * vsig_b * vr, 0.f);
-        float AVPa = P_a + qa, AVPb = (Eb.x + Eb.y) + qb;
-        float f    = AVPa * c1a * Fa + AVPb * Eb.z * Fb;
-        kahan_add(Fx, cx, f * rx);
-        kahan_add(Fy, cy, f * ry);
-        kahan_add(Fz, cz, f * rz);
-        float du = AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - Cb.w) * (Fa * c2a + Fb * Eb.w);
-        kahan_add(U, cu, du);
-        vsig_max = fmaxf(vsig_max, cs_a + 2.f * avr);
+    for (u32 k = k0; k < k1; k += 4) {
+        u32 bb[4];
+        float4 Ab[4], Bb[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) bb[j] = (k + j < k1) ? __ldg(&rs.ent[k + j]) : a;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            Ab[j] = __ldg(&ms.P[2 * (size_t) bb[j]]);
+            Bb[j] = __ldg(&ms.P[2 * (size_t) bb[j] + 1]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float dx = (Aa.x - Ab[j].x) + (Ba.x - Bb[j].x);
+            float dy = (Aa.y - Ab[j].y) + (Ba.y - Bb[j].y);
+            float dz = (Aa.z - Ab[j].z) + (Ba.z - Bb[j].z);
+            float r2 = dx * dx + dy * dy + dz * dz;
+            float hib = Ab[j].w;
+            if ((r2 * hia2 > 4.f && r2 * hib * hib > 4.f) || r2 == 0.f) continue;
+            const float4 *hb = &ms.H[3 * (size_t) bb[j]];
+            float4 Cb = __ldg(hb), Db = __ldg(hb + 1), Eb = __ldg(hb + 2);
+            float rinv = rsqrtf(r2);
+            float rab  = r2 * rinv;
+            float Fa   = k4a * m4_df32(rab * hia);
+            float Fb   = hib * hib * hib * hib * kNorm3dF * m4_df32(rab * hib);
+            float rx = dx * rinv, ry = dy * rinv, rz = dz * rinv;
+            float vx = (Ca.x - Cb.x) + (Da.x - Db.x);
+            float vy = (Ca.y - Cb.y) + (Da.y - Db.y);
+            float vz = (Ca.z - Cb.z) + (Da.z - Db.z);
+            float vr  = vx * rx + vy * ry + vz * rz;
+            float avr = fabsf(vr);
+            float rho_b = Db.w, cs_b = Bb[j].w;
+            float vsig_a = p.alpha_AV * cs_a + p.beta_AV * avr;
+            float vsig_b = p.alpha_AV * cs_b + p.beta_AV * avr;
+            float dP     = (Ea.x - Eb.x) + (Ea.y - Eb.y);
+            float vsig_u = sqrtf(fabsf(dP) / ((rho_a + rho_b) * 0.5f));
+            float qa = fmaxf(-0.5f * rho_a * vsig_a * vr, 0.f);
+            float qb = fmaxf(-0.5f * rho_b * vsig_b * vr, 0.f);
+            float AVPa = P_a + qa, AVPb = (Eb.x + Eb.y) + qb;
+            float f    = AVPa * c1a * Fa + AVPb * Eb.z * Fb;
+            kahan_add(Fx, cx, f * rx);
+            kahan_add(Fy, cy, f * ry);
+            kahan_add(Fz, cz, f * rz);
+            float du = AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - Cb.w) * (Fa * c2a + Fb * Eb.w);
+            kahan_add(U, cu, du);
+            vsig_max = fmaxf(vsig_max, cs_a + 2.f * avr);
+        }
     }
 }
 
@@ -285,30 +311,28 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
     }
 }
 
+// f_pos holds 2N float4 (position records), f_aux0 3N float4 (hydro records)
 MixedSpace mixed_space(Ctx &c, u32 N) {
-    float4 *base = c.f_pos.as<float4>();
-    return MixedSpace{base, base + N, c.f_aux0.as<float4>(), c.f_aux1.as<float4>(),
-                      c.f_aux2.as<float4>()};
+    return MixedSpace{c.f_pos.as<float4>(), c.f_aux0.as<float4>()};
 }
 
 cudaError_t ensure_mixed(Ctx &c, u32 N) {
     cudaError_t e;
     if ((e = c.f_pos.ensure(2 * sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
-    if ((e = c.f_aux0.ensure(sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
-    if ((e = c.f_aux1.ensure(sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
-    return c.f_aux2.ensure(sizeof(float4) * (size_t) N, c.stream);
+    return c.f_aux0.ensure(3 * sizeof(float4) * (size_t) N, c.stream);
 }
 
 } // namespace
 
+const float4 *mixed_positions(Ctx &c) { return c.f_pos.as<float4>(); }
+
 cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol) {
     cudaError_t e = ensure_mixed(c, N);
     if (e != cudaSuccess) return e;
-    MixedSpace ms = mixed_space(c, N);
     ProfScope ps(c, kProfTree, N);
     { k_stage_pos<<<div_up(N, 256), 256, 0, c.stream>>>(N, c.sx.as<f64>(), c.sy.as<f64>(),
                                                       c.sz.as<f64>(), c.sh.as<f64>(), h_tol,
-                                                      (float4 *) ms.A, (float4 *) ms.B); GBSPH_COUNTED; }
+                                                      c.f_pos.as<float4>()); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 
@@ -337,9 +361,8 @@ cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, 
     {
         ProfScope ps(c, kProfGatherEos, N);
         { k_stage_hydro<<<div_up(N, 256), 256, 0, c.stream>>>(N, nullptr, nullptr, nullptr, hs, pmass,
-                                                            (float4 *) ms.A, (float4 *) ms.B,
-                                                            (float4 *) ms.C, (float4 *) ms.D,
-                                                            (float4 *) ms.E); GBSPH_COUNTED; }
+                                                            c.f_pos.as<float4>(),
+                                                            c.f_aux0.as<float4>()); GBSPH_COUNTED; }
     }
     MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
     ProfScope ps(c, kProfDerivs, rs.n);
@@ -352,15 +375,14 @@ cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, 
 cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                                 f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
                                 f64 *du, f64 *vsig) {
-    // merged count = 1 + largest entry; the caller's merged arrays are sized by it
+    // the caller's merged arrays hold c.n_obj entries (set from n_merged)
     u32 N = c.n_obj;
     cudaError_t e = ensure_mixed(c, N);
     if (e != cudaSuccess) return e;
     MixedSpace ms = mixed_space(c, N);
     { k_stage_hydro<<<div_up(N, 256), 256, 0, c.stream>>>(N, rs.x, rs.y, rs.z, hs, pmass,
-                                                        (float4 *) ms.A, (float4 *) ms.B,
-                                                        (float4 *) ms.C, (float4 *) ms.D,
-                                                        (float4 *) ms.E); GBSPH_COUNTED; }
+                                                        c.f_pos.as<float4>(),
+                                                        c.f_aux0.as<float4>()); GBSPH_COUNTED; }
     MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
     { k_derivs_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, ax, ay, az, du, vsig); GBSPH_COUNTED; }
     return cudaGetLastError();
@@ -410,12 +432,13 @@ extern "C" int gbsph_derivs_constAV_mixed_noalloc(
     }
     float4 *b     = g_noalloc_base[dev];
     u32 N         = n_merged;
-    MixedSpace ms{b, b + N, b + 2 * (size_t) N, b + 3 * (size_t) N, b + 4 * (size_t) N};
+    // 2N position records then 3N hydro records
+    MixedSpace ms{b, b + 2 * (size_t) N};
     RowSpace rs{n_local, nullptr, nullptr, cnt, scanned, entries, x, y, z};
     HydroSpace hs{h, u, vx, vy, vz, omega, P, cs};
     cudaStream_t s = (cudaStream_t) stream;
     // every staging entry the pair kernel reads is rewritten first: nothing to clear
-    { k_stage_hydro<<<div_up(N, 256), 256, 0, s>>>(N, x, y, z, hs, pmass, b, b + N, b + 2 * (size_t) N, b + 3 * (size_t) N, b + 4 * (size_t) N); GBSPH_COUNTED; }
+    { k_stage_hydro<<<div_up(N, 256), 256, 0, s>>>(N, x, y, z, hs, pmass, b, b + 2 * (size_t) N); GBSPH_COUNTED; }
     MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
     { k_derivs_mixed<<<div_up(n_local, 128), 128, 0, s>>>(rs, ms, p, pmass, ax, ay, az, du, vsig); GBSPH_COUNTED; }
     return cudaGetLastError() == cudaSuccess ? GBSPH_OK : GBSPH_ERR_CUDA;

@@ -5,19 +5,24 @@
 
 namespace gbsph {
 
-// Rank-ordered FP32 staging of merged fields for the mixed pair kernels, five
-// float4 per particle (80 bytes):
-//   A = {x_hi, y_hi, z_hi, 1/h}      B = {x_lo, y_lo, z_lo, c_s}
-//   C = {vx_hi, vy_hi, vz_hi, u}     D = {vx_lo, vy_lo, vz_lo, rho}
-//   E = {P_hi, P_lo, 1/(rho^2 Omega), 1/(rho Omega)}
+// Rank-ordered FP32 staging of merged fields for the mixed pair kernels, five float4
+// (80 bytes) per particle in two records:
+//   position record P[2r], P[2r+1] (32 B, one sector):
+//     A = {x_hi, y_hi, z_hi, 1/h}      B = {x_lo, y_lo, z_lo, c_s}
+//   hydro record H[3r .. 3r+2] (48 B, two sectors):
+//     C = {vx_hi, vy_hi, vz_hi, u}     D = {vx_lo, vy_lo, vz_lo, rho}
+//     E = {P_hi, P_lo, 1/(rho^2 Omega), 1/(rho Omega)}
 // A position is carried as an unevaluated sum hi + lo of two floats (hi = fl32(x),
 // lo = fl32(x - hi)), so a pair separation (hi_a - hi_b) + (lo_a - lo_b) is accurate
 // to FP32 rounding of the separation itself, wherever the particles sit in the box.
 struct MixedSpace {
-    const float4 *A, *B, *C, *D, *E;
+    const float4 *P; // 2 per particle
+    const float4 *H; // 3 per particle
 };
 
 cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol);
+// the position records staged by stage_positions_mixed (B.w = fl32 cache threshold)
+const float4 *mixed_positions(Ctx &c);
 cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
                             f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters);
 cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
