@@ -205,7 +205,7 @@ int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *sc
  * no counterpart in the reference.  Needs no context: it runs on the current device
  * and takes the same inputs, outputs and results as the context entry point.
  *  - The FP32 staging lives in a fixed device array inside the library, sized for at
- *    most 65,536 merged particles (5 MiB, reserved on every GPU that loads the library
+ *    most 65,536 merged particles (4 MiB, reserved on every GPU that loads the library
  *    until the process exits); larger n_merged returns GBSPH_ERR_CAPACITY.
  *  - The first call on a device looks the array's device address up; make that first
  *    call before any stream capture.

@@ -26,6 +26,8 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
                  "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
 # FP64 units whose results are compared bit for bit with the oracle
 EXACT = {"tree.cu", "neigh.cu", "ghosts.cu", "sph64.cu", "scan.cu", "driver.cu", "adjoint.cu"}
+# FP32-mixed pair kernels: approximate FP32 division / square root, denormals flushed
+FAST32 = {"sph_mixed.cu"}
 
 
 def nvcc():
@@ -50,6 +52,8 @@ def _compile(src):
     obj = os.path.join(BUILD, src.replace(".cu", ".o"))
     flags = list(COMMON)
     flags += ["-fmad=false"] if src in EXACT else ["-fmad=true"]
+    if src in FAST32:
+        flags += ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
     if os.environ.get("GBSPH_PTXAS_VERBOSE"):
         flags += ["-Xptxas", "-v"]
     cmd = [nvcc()] + flags + ["-c", os.path.join(CSRC, src), "-o", obj]

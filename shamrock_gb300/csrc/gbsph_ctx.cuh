@@ -48,7 +48,8 @@ enum KernelFlags : u32 {
 };
 
 // FP32 copy of a node box for pre-tests: lo.w = interaction radius x Rkern.
-struct __align__(16) NodeBoxF {
+// 32 bytes, read with one 256-bit load.
+struct __align__(32) NodeBoxF {
     float4 lo;
     float4 hi;
 };

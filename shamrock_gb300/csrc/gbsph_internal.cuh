@@ -55,6 +55,21 @@ __device__ __forceinline__ f64 dot3_rn(f64 x, f64 y, f64 z) {
     return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
 }
 
+// ------------------------------------------------------------------ wide loads
+// A 32-byte record fetched with one 256-bit read-only load (sm_100 and later): one L1
+// request per lane instead of two 128-bit ones.  The pointer must be 32-byte aligned.
+struct __align__(32) F8 {
+    float4 a, b;
+};
+__device__ __forceinline__ F8 ldg256(const void *p) {
+    F8 r;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y),
+          "=f"(r.b.z), "=f"(r.b.w)
+        : "l"(p));
+    return r;
+}
+
 // double <-> order-preserving u64 (for atomic min/max on doubles)
 __device__ __forceinline__ u64 f64_to_ordered(f64 v) {
     u64 b = (u64) __double_as_longlong(v);

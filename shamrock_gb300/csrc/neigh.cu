@@ -147,15 +147,16 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
     u32 c = 0, base = l * kLeafCap;
     bool ok;
     if (fb) {
-        float4 alo = __ldg(&fb[t.off() + l].lo), ahi = __ldg(&fb[t.off() + l].hi);
-        float4 rlo = __ldg(&fb[0].lo), rhi = __ldg(&fb[0].hi);
+        F8 fa = ldg256(&fb[t.off() + l]), fr = ldg256(&fb[0]);
+        const float4 alo = fa.a, ahi = fa.b, rlo = fr.a, rhi = fr.b;
         float M = fmaxf(fmaxf(fmaxf(fabsf(rlo.x), fabsf(rlo.y)), fmaxf(fabsf(rlo.z), fabsf(rhi.x))),
                         fmaxf(fabsf(rhi.y), fabsf(rhi.z)));
         float band_abs = 1e-6f * M;
         ok = dfs(
             t,
             [&](u32 node) {
-                float4 nlo = __ldg(&fb[node].lo), nhi = __ldg(&fb[node].hi);
+                F8 fn = ldg256(&fb[node]);
+                const float4 nlo = fn.a, nhi = fn.b;
                 float sx = fmaxf(nlo.x - ahi.x, alo.x - nhi.x);
                 float sy = fmaxf(nlo.y - ahi.y, alo.y - nhi.y);
                 float sz = fmaxf(nlo.z - ahi.z, alo.z - nhi.z);
@@ -239,9 +240,11 @@ __global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows
 }
 
 // ---- stage 2 (NeighbourCache.cpp:492-591)
-// MODE kCount: per-row count; kFill: entries at off[row] (compact CSR after a scan);
-// kOnePass: entries straight into kRowCap slots per row (off[row] = row * kRowCap),
-// flagging kFlagCsrCap when a row overflows so the host reruns the two-pass build.
+// MODE kCount: per-row count, and the count rounded up to 4 into off[] (scanned in
+// place into offsets); kFill: entries at off[row]; kOnePass: entries straight into
+// kRowCap slots per row (off[row] = row * kRowCap), flagging kFlagCsrCap when a row
+// overflows so the host reruns the two-pass build.  Either way every row starts on a
+// 16-byte boundary, so readers may fetch entries four at a time.
 //
 // F32: the pair test is r^2 <= max(thr_a, thr_b), thr = ((h htol)^2) R^2 in FP64.  r^2
 // is estimated in FP32 from hi/lo-split positions (relative error below ~3e-7) and
@@ -267,8 +270,9 @@ __global__ void __launch_bounds__(256) k_part_cache(
         f64 thr_a  = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
         float4 Aa = make_float4(0, 0, 0, 0), Ba = Aa;
         if (F32) {
-            Aa = __ldg(&P[2 * (size_t) ra]);
-            Ba = __ldg(&P[2 * (size_t) ra + 1]);
+            F8 pa = ldg256(&P[2 * (size_t) ra]);
+            Aa    = pa.a;
+            Ba    = pa.b;
         }
         const float lo_f = 1.f - 1e-5f, hi_f = 1.f + 1e-5f;
         u32 leaf = owner[row];
@@ -280,7 +284,8 @@ __global__ void __launch_bounds__(256) k_part_cache(
             for (u32 rb = r0; rb < r1; rb++) {
                 int decided = -1;
                 if (F32) {
-                    float4 Ab = __ldg(&P[2 * (size_t) rb]), Bb = __ldg(&P[2 * (size_t) rb + 1]);
+                    F8 pb = ldg256(&P[2 * (size_t) rb]);
+                    const float4 Ab = pb.a, Bb = pb.b;
                     float dx = __fadd_rn(__fsub_rn(Aa.x, Ab.x), __fsub_rn(Ba.x, Bb.x));
                     float dy = __fadd_rn(__fsub_rn(Aa.y, Ab.y), __fsub_rn(Ba.y, Bb.y));
                     float dz = __fadd_rn(__fsub_rn(Aa.z, Ab.z), __fsub_rn(Ba.z, Bb.z));
@@ -307,12 +312,13 @@ __global__ void __launch_bounds__(256) k_part_cache(
             }
         }
         if (MODE != kFill) cnt[row] = c;
+        if (MODE == kCount) off[row] = (c + 3u) & ~3u;
         if (MODE == kOnePass) {
             off[row] = w;
             if (c > kRowCap) atomicOr(&sc->flags, kFlagCsrCap);
         }
     }
-    if (MODE == kOnePass) {
+    if (MODE != kCount) {
         u64 tot = block_reduce((u64) c, OpAddU64{}, 0ull);
         if (threadIdx.x == 0) atomicAdd((unsigned long long *) &sc->csr_entries, (unsigned long long) tot);
     }
@@ -441,7 +447,7 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     // the padded one-pass layout needs row * kRowCap to fit the u32 offsets
     const bool one_pass = (u64) n * kRowCap < 0xffffffffull;
     if (one_pass)
-        if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * kRowCap + 1), s)) != cudaSuccess) return e;
+        if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * kRowCap + 4), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(&dsc->csr_entries, 0, sizeof(u64), s)) != cudaSuccess) return e;
     // launch helper for the stage-2 kernel family
     auto part = [&](auto mode_tag, u32 *cnt, u32 *off, u32 *ent) {
@@ -472,16 +478,22 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         // a row has more than kRowCap entries: two-pass build into a compact CSR
         {
             ProfScope ps(c, kProfCacheCount, n);
-            part(Count{}, c.csr_cnt.as<u32>(), nullptr, nullptr);
+            part(Count{}, c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), nullptr);
         }
-        if ((e = scan_exclusive_u32(c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), n, &dsc->total,
+        // rows padded to multiples of 4 entries, scanned in place
+        if ((e = scan_exclusive_u32(c.csr_off.as<u32>(), c.csr_off.as<u32>(), n, &dsc->total,
                                     c.scan_scratch, s)) != cudaSuccess)
             return e;
+        if ((e = cudaMemsetAsync(&dsc->csr_entries, 0, sizeof(u64), s)) != cudaSuccess) return e;
         if ((e = sync_scalars(c)) != cudaSuccess) return e;
-        c.csr_total = c.h_scalars->total;
-        if ((e = c.csr_ent.ensure(sizeof(u32) * (c.csr_total + 1), s)) != cudaSuccess) return e;
-        ProfScope ps(c, kProfCacheFill, 0);
-        part(Fill{}, nullptr, c.csr_off.as<u32>(), c.csr_ent.as<u32>());
+        u64 padded = c.h_scalars->total;
+        if ((e = c.csr_ent.ensure(sizeof(u32) * (padded + 4), s)) != cudaSuccess) return e;
+        {
+            ProfScope ps(c, kProfCacheFill, 0);
+            part(Fill{}, nullptr, c.csr_off.as<u32>(), c.csr_ent.as<u32>());
+        }
+        if ((e = sync_scalars(c)) != cudaSuccess) return e;
+        c.csr_total = c.h_scalars->csr_entries;
     }
     c.cache_valid = true;
     return cudaGetLastError();

@@ -3,7 +3,8 @@
 // shamalgs/src/details/numeric/numeric.cpp:48-92).
 //
 // Reduce-then-scan in three launches: per-tile totals, one block scanning the tile
-// totals, per-tile scan plus tile offset.  A tile is 256 threads x 8 items.
+// totals, per-tile scan plus tile offset.  A tile is 256 threads x 8 items.  Each item is
+// read and written by the same thread, so the u32 scan may run in place (in == out).
 
 #include "gbsph_internal.cuh"
 

@@ -10,7 +10,9 @@ namespace gbsph {
 //    ids, positions are indexed by merged id; row_rank == row_local == nullptr.
 //  - pipeline form: row t is the t-th local particle in Morton order,
 //    row_rank[t] its rank, row_local[t] its local id; entries are ranks and
-//    positions are the rank-ordered copies.
+//    positions are the rank-ordered copies.  Rows come from the library's own cache:
+//    each starts on a 4-entry boundary and its slot is padded to a multiple of 4, so
+//    entries may be read four at a time.
 struct RowSpace {
     u32 n;
     const u32 *row_rank;

@@ -5,10 +5,16 @@
 // leapfrog corrector and CFL, and the global totals.  Same physics and neighbour
 // set as the FP64 kernels (sph64.cu); see those for the reference citations.
 //
-// Neighbour loops take CSR entries four at a time and issue the four position-record
-// loads together, so several L2 round trips are in flight per thread.
+// Every neighbour costs one 256-bit load of its position record (density sums) or
+// two (derivatives: position + hydro record).  Neighbour loops take CSR entries four
+// at a time, issue all record loads of the four together and fetch the next four
+// entries behind them, so each batch waits on one round trip.  Sums are accumulated
+// per batch in plain FP32 and the batch sums are Kahan-compensated.  This unit is
+// compiled with approximate FP32 division and square root (about 2 ulp).
 
 #include "sph_mixed.cuh"
+
+#include <cuda_bf16.h>
 
 namespace gbsph {
 
@@ -34,8 +40,38 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 __device__ __forceinline__ float hi32(f64 v) { return __double2float_rn(v); }
 __device__ __forceinline__ float lo32(f64 v) { return __double2float_rn(v - (f64) __double2float_rn(v)); }
 
+// Two residuals in one 32-bit word as bfloat16 (8 exponent bits: the range of a float,
+// so no residual underflows): with hi = fl32(v) the pair hi + bf16(lo) carries v to
+// about 2^-33 relative.
+__device__ __forceinline__ float pack_bf16x2(float a, float b) {
+    u32 ha = __bfloat16_as_ushort(__float2bfloat16_rn(a));
+    u32 hb = __bfloat16_as_ushort(__float2bfloat16_rn(b));
+    return __uint_as_float((ha << 16) | hb);
+}
+__device__ __forceinline__ float bf_hi(float w) { return __uint_as_float(__float_as_uint(w) & 0xffff0000u); }
+__device__ __forceinline__ float bf_lo(float w) { return __uint_as_float(__float_as_uint(w) << 16); }
+
 __device__ __forceinline__ f64 rho_h64(f64 m, f64 h) {
     return m * (kHfact / h) * (kHfact / h) * (kHfact / h);
+}
+
+// Four CSR entries from k on as a uint4, slots at or past k1 set to `pad`.  vec: the row
+// is padded to 4-entry boundaries (library cache) and is read with one 128-bit load.
+__device__ __forceinline__ uint4 load_entries(const u32 *__restrict__ ent, u32 k, u32 k1, bool vec,
+                                              u32 pad) {
+    uint4 v;
+    if (vec) {
+        v = __ldg((const uint4 *) (ent + k));
+    } else {
+        v.x = __ldg(&ent[k]);
+        v.y = (k + 1 < k1) ? __ldg(&ent[k + 1]) : pad;
+        v.z = (k + 2 < k1) ? __ldg(&ent[k + 2]) : pad;
+        v.w = (k + 3 < k1) ? __ldg(&ent[k + 3]) : pad;
+    }
+    if (k + 1 >= k1) v.y = pad;
+    if (k + 2 >= k1) v.z = pad;
+    if (k + 3 >= k1) v.w = pad;
+    return v;
 }
 
 // B.w carries fl32 of the neighbour-cache threshold ((h htol)^2) R^2 (computed in FP64
@@ -62,7 +98,7 @@ __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__res
     f64 h = hs.h[r], om = hs.omega[r], Pr = hs.P[r];
     f64 rho = rho_h64(pmass, h);
     float hinv = __double2float_rn(1.0 / h);
-    size_t p2 = 2 * (size_t) r, h3 = 3 * (size_t) r;
+    size_t p2 = 2 * (size_t) r;
     if (x) {
         P[p2]     = make_float4(hi32(x[r]), hi32(y[r]), hi32(z[r]), hinv);
         P[p2 + 1] = make_float4(lo32(x[r]), lo32(y[r]), lo32(z[r]), __double2float_rn(hs.cs[r]));
@@ -71,48 +107,50 @@ __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__res
         ((float *) &P[p2 + 1])[3] = __double2float_rn(hs.cs[r]);
     }
     f64 vx = hs.vx[r], vy = hs.vy[r], vz = hs.vz[r];
-    H[h3]     = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(hs.u[r]));
-    H[h3 + 1] = make_float4(lo32(vx), lo32(vy), lo32(vz), __double2float_rn(rho));
     f64 sub = rho * rho * om;
     f64 c1  = (sub != 0 && sub == sub) ? 1. / sub : 0.;
-    H[h3 + 2] = make_float4(hi32(Pr), lo32(Pr), __double2float_rn(c1), __double2float_rn(1. / (rho * om)));
+    H[p2]     = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(hs.u[r]));
+    H[p2 + 1] = make_float4(hi32(Pr), __double2float_rn(c1), pack_bf16x2(lo32(vx), lo32(vy)),
+                            pack_bf16x2(lo32(vz), lo32(Pr)));
 }
 
-// sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a
+// sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a.  The next four entries
+// are fetched while the current four position records are in flight.
 __device__ __forceinline__ void density_sums_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
                                                  u32 k0, u32 k1, float hinv, float &sf, float &sg) {
-    float4 Aa = __ldg(&ms.P[2 * (size_t) a]), Ba = __ldg(&ms.P[2 * (size_t) a + 1]);
+    const F8 pa    = ldg256(&ms.P[2 * (size_t) a]);
+    const bool vec = rs.row_rank != nullptr;
     float cf = 0.f, cg = 0.f;
     sf = 0.f;
     sg = 0.f;
     float hinv2 = hinv * hinv;
+    uint4 nx    = (k0 < k1) ? load_entries(rs.ent, k0, k1, vec, a) : make_uint4(a, a, a, a);
     for (u32 k = k0; k < k1; k += 4) {
-        u32 bb[4];
-        float4 Ab[4], Bb[4];
+        const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
+        F8 pb[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) bb[j] = (k + j < k1) ? __ldg(&rs.ent[k + j]) : a;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            Ab[j] = __ldg(&ms.P[2 * (size_t) bb[j]]);
-            Bb[j] = __ldg(&ms.P[2 * (size_t) bb[j] + 1]);
-        }
+        for (int j = 0; j < 4; j++) pb[j] = ldg256(&ms.P[2 * (size_t) bb[j]]);
+        if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, vec, a);
+        float bf = 0.f, bg = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            float dx = (Aa.x - Ab[j].x) + (Ba.x - Bb[j].x);
-            float dy = (Aa.y - Ab[j].y) + (Ba.y - Bb[j].y);
-            float dz = (Aa.z - Ab[j].z) + (Ba.z - Bb[j].z);
+            float dx = (pa.a.x - pb[j].a.x) + (pa.b.x - pb[j].b.x);
+            float dy = (pa.a.y - pb[j].a.y) + (pa.b.y - pb[j].b.y);
+            float dz = (pa.a.z - pb[j].a.z) + (pa.b.z - pb[j].b.z);
             float q2 = (dx * dx + dy * dy + dz * dz) * hinv2;
             if (k + j >= k1 || q2 > 4.f) continue;
             float q  = sqrtf(q2);
             float f  = m4_f32(q);
             float df = m4_df32(q);
-            kahan_add(sf, cf, f);
-            kahan_add(sg, cg, 3.f * f + q * df);
+            bf += f;
+            bg += 3.f * f + q * df;
         }
+        kahan_add(sf, cf, bf);
+        kahan_add(sg, cg, bg);
     }
 }
 
-__global__ void __launch_bounds__(256) k_h_iterate_mixed(RowSpace rs, MixedSpace ms,
+__global__ void __launch_bounds__(256, 4) k_h_iterate_mixed(RowSpace rs, MixedSpace ms,
                                                          const f64 *__restrict__ h_old,
                                                          f64 *__restrict__ h_new,
                                                          f64 *__restrict__ eps, f64 pmass,
@@ -178,73 +216,85 @@ __global__ void __launch_bounds__(256) k_omega_mixed(RowSpace rs, MixedSpace ms,
 
 struct MixedParams {
     float alpha_u, alpha_AV, beta_AV;
+    float mh3; // m hfact^3: rho = mh3 / h^3
 };
 
 // FP32 pair loop of the constant-AV derivatives; returns the bare sums
 //   F = sum (ca Fa + cb Fb) r_hat   (acceleration = -m F)
 //   U = sum [AVPa c1a Fa (v.r_hat) + 0.5 alpha_u vsig_u (u_a - u_b)(Fa c2a + Fb c2b)]
-//   (du/dt = m U), and the v_sig maximum of the reference's separate v_sig kernel.
+//   (du/dt = m U), and the v_sig maximum of the reference's separate v_sig kernel,
+// with c1 = 1/(rho^2 Omega) and c2 = 1/(rho Omega) = c1 rho, rho = m (hfact/h)^3.
 // Self and coincident pairs (r = 0) contribute nothing and are skipped, which also
 // makes padding a partial batch of four with the row's own index harmless.
 __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
                                                u32 k0, u32 k1, const MixedParams &p, float &Fx,
                                                float &Fy, float &Fz, float &U, float &vsig_max) {
-    float4 Aa = __ldg(&ms.P[2 * (size_t) a]), Ba = __ldg(&ms.P[2 * (size_t) a + 1]);
-    float4 Ca = __ldg(&ms.H[3 * (size_t) a]), Da = __ldg(&ms.H[3 * (size_t) a + 1]),
-           Ea = __ldg(&ms.H[3 * (size_t) a + 2]);
-    const float hia = Aa.w, cs_a = Ba.w, u_a = Ca.w, rho_a = Da.w;
-    const float P_a = Ea.x + Ea.y, c1a = Ea.z, c2a = Ea.w;
-    const float k4a = hia * hia * hia * hia * kNorm3dF;
+    const bool vec = rs.row_rank != nullptr;
+    const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
+    const F8 ha = ldg256(&ms.H[2 * (size_t) a]);
+    const float hia = pa.a.w, cs_a = pa.b.w, u_a = ha.a.w;
     const float hia2 = hia * hia;
+    const float rho_a = p.mh3 * hia2 * hia;
+    const float Pa_hi = ha.b.x, Pa_lo = bf_lo(ha.b.w), P_a = Pa_hi + Pa_lo;
+    const float c1a = ha.b.y, c2a = c1a * rho_a;
+    const float vla_x = bf_hi(ha.b.z), vla_y = bf_lo(ha.b.z), vla_z = bf_hi(ha.b.w);
+    const float k4a = hia2 * hia2 * kNorm3dF;
     float cx = 0.f, cy = 0.f, cz = 0.f, cu = 0.f;
     Fx = Fy = Fz = U = 0.f;
     vsig_max = 0.f;
+    uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, vec, a) : make_uint4(a, a, a, a);
     for (u32 k = k0; k < k1; k += 4) {
-        u32 bb[4];
-        float4 Ab[4], Bb[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) bb[j] = (k + j < k1) ? __ldg(&rs.ent[k + j]) : a;
+        // both records of all four neighbours in one round trip, next entries behind them
+        const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
+        F8 pb[4], hb[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            Ab[j] = __ldg(&ms.P[2 * (size_t) bb[j]]);
-            Bb[j] = __ldg(&ms.P[2 * (size_t) bb[j] + 1]);
+            pb[j] = ldg256(&ms.P[2 * (size_t) bb[j]]);
+            hb[j] = ldg256(&ms.H[2 * (size_t) bb[j]]);
         }
+        if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, vec, a);
+        float bx = 0.f, by = 0.f, bz = 0.f, bu = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            float dx = (Aa.x - Ab[j].x) + (Ba.x - Bb[j].x);
-            float dy = (Aa.y - Ab[j].y) + (Ba.y - Bb[j].y);
-            float dz = (Aa.z - Ab[j].z) + (Ba.z - Bb[j].z);
+            float dx = (pa.a.x - pb[j].a.x) + (pa.b.x - pb[j].b.x);
+            float dy = (pa.a.y - pb[j].a.y) + (pa.b.y - pb[j].b.y);
+            float dz = (pa.a.z - pb[j].a.z) + (pa.b.z - pb[j].b.z);
             float r2 = dx * dx + dy * dy + dz * dz;
-            float hib = Ab[j].w;
-            if ((r2 * hia2 > 4.f && r2 * hib * hib > 4.f) || r2 == 0.f) continue;
-            const float4 *hb = &ms.H[3 * (size_t) bb[j]];
-            float4 Cb = __ldg(hb), Db = __ldg(hb + 1), Eb = __ldg(hb + 2);
+            const float hib = pb[j].a.w, cs_b = pb[j].b.w;
+            const float hib2 = hib * hib;
+            if (k + j >= k1 || r2 == 0.f || (r2 * hia2 > 4.f && r2 * hib2 > 4.f)) continue;
+            const float hib3 = hib2 * hib;
+            const float rho_b = p.mh3 * hib3;
+            const float c1b = hb[j].b.y, c2b = c1b * rho_b;
+            const float Pb_lo = bf_lo(hb[j].b.w), P_b = hb[j].b.x + Pb_lo;
             float rinv = rsqrtf(r2);
             float rab  = r2 * rinv;
             float Fa   = k4a * m4_df32(rab * hia);
-            float Fb   = hib * hib * hib * hib * kNorm3dF * m4_df32(rab * hib);
+            float Fb   = hib3 * hib * kNorm3dF * m4_df32(rab * hib);
             float rx = dx * rinv, ry = dy * rinv, rz = dz * rinv;
-            float vx = (Ca.x - Cb.x) + (Da.x - Db.x);
-            float vy = (Ca.y - Cb.y) + (Da.y - Db.y);
-            float vz = (Ca.z - Cb.z) + (Da.z - Db.z);
+            float vx = (ha.a.x - hb[j].a.x) + (vla_x - bf_hi(hb[j].b.z));
+            float vy = (ha.a.y - hb[j].a.y) + (vla_y - bf_lo(hb[j].b.z));
+            float vz = (ha.a.z - hb[j].a.z) + (vla_z - bf_hi(hb[j].b.w));
             float vr  = vx * rx + vy * ry + vz * rz;
             float avr = fabsf(vr);
-            float rho_b = Db.w, cs_b = Bb[j].w;
             float vsig_a = p.alpha_AV * cs_a + p.beta_AV * avr;
             float vsig_b = p.alpha_AV * cs_b + p.beta_AV * avr;
-            float dP     = (Ea.x - Eb.x) + (Ea.y - Eb.y);
+            float dP     = (Pa_hi - hb[j].b.x) + (Pa_lo - Pb_lo);
             float vsig_u = sqrtf(fabsf(dP) / ((rho_a + rho_b) * 0.5f));
             float qa = fmaxf(-0.5f * rho_a * vsig_a * vr, 0.f);
             float qb = fmaxf(-0.5f * rho_b * vsig_b * vr, 0.f);
-            float AVPa = P_a + qa, AVPb = (Eb.x + Eb.y) + qb;
-            float f    = AVPa * c1a * Fa + AVPb * Eb.z * Fb;
-            kahan_add(Fx, cx, f * rx);
-            kahan_add(Fy, cy, f * ry);
-            kahan_add(Fz, cz, f * rz);
-            float du = AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - Cb.w) * (Fa * c2a + Fb * Eb.w);
-            kahan_add(U, cu, du);
+            float AVPa = P_a + qa, AVPb = P_b + qb;
+            float f    = AVPa * c1a * Fa + AVPb * c1b * Fb;
+            bx += f * rx;
+            by += f * ry;
+            bz += f * rz;
+            bu += AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - hb[j].a.w) * (Fa * c2a + Fb * c2b);
             vsig_max = fmaxf(vsig_max, cs_a + 2.f * avr);
         }
+        kahan_add(Fx, cx, bx);
+        kahan_add(Fy, cy, by);
+        kahan_add(Fz, cz, bz);
+        kahan_add(U, cu, bu);
     }
 }
 
@@ -311,7 +361,12 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
     }
 }
 
-// f_pos holds 2N float4 (position records), f_aux0 3N float4 (hydro records)
+MixedParams mixed_params(f64 pmass, f64 alpha_u, f64 alpha_AV, f64 beta_AV) {
+    f64 mh3 = pmass * kHfact * kHfact * kHfact;
+    return MixedParams{(float) alpha_u, (float) alpha_AV, (float) beta_AV, (float) mh3};
+}
+
+// f_pos holds 2N float4 (position records), f_aux0 2N float4 (hydro records)
 MixedSpace mixed_space(Ctx &c, u32 N) {
     return MixedSpace{c.f_pos.as<float4>(), c.f_aux0.as<float4>()};
 }
@@ -319,7 +374,7 @@ MixedSpace mixed_space(Ctx &c, u32 N) {
 cudaError_t ensure_mixed(Ctx &c, u32 N) {
     cudaError_t e;
     if ((e = c.f_pos.ensure(2 * sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
-    return c.f_aux0.ensure(3 * sizeof(float4) * (size_t) N, c.stream);
+    return c.f_aux0.ensure(2 * sizeof(float4) * (size_t) N, c.stream);
 }
 
 } // namespace
@@ -364,7 +419,7 @@ cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, 
                                                             c.f_pos.as<float4>(),
                                                             c.f_aux0.as<float4>()); GBSPH_COUNTED; }
     }
-    MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
+    MixedParams p = mixed_params(pmass, alpha_u, alpha_AV, beta_AV);
     ProfScope ps(c, kProfDerivs, rs.n);
     { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, hs.h, hdt, C_cour,
                                                                  C_force, lf,
@@ -383,7 +438,7 @@ cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs
     { k_stage_hydro<<<div_up(N, 256), 256, 0, c.stream>>>(N, rs.x, rs.y, rs.z, hs, pmass,
                                                         c.f_pos.as<float4>(),
                                                         c.f_aux0.as<float4>()); GBSPH_COUNTED; }
-    MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
+    MixedParams p = mixed_params(pmass, alpha_u, alpha_AV, beta_AV);
     { k_derivs_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, ax, ay, az, du, vsig); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
@@ -398,9 +453,9 @@ namespace {
 
 // Largest merged (locals + ghosts) particle count the fixed staging holds.
 constexpr u32 kNoAllocMaxMerged = 1u << 16;
-// Five float4 per merged particle: 65,536 x 80 B = 5 MiB, reserved on every GPU that
+// Four float4 per merged particle: 65,536 x 64 B = 4 MiB, reserved on every GPU that
 // loads the library and kept until the process exits.
-static __device__ __align__(256) float4 g_noalloc_staging[5 * kNoAllocMaxMerged];
+static __device__ __align__(256) float4 g_noalloc_staging[4 * kNoAllocMaxMerged];
 
 constexpr int kNoAllocMaxDevices = 64;
 float4 *g_noalloc_base[kNoAllocMaxDevices] = {};
@@ -432,14 +487,14 @@ extern "C" int gbsph_derivs_constAV_mixed_noalloc(
     }
     float4 *b     = g_noalloc_base[dev];
     u32 N         = n_merged;
-    // 2N position records then 3N hydro records
+    // N position records (2N float4) then N hydro records (2N float4)
     MixedSpace ms{b, b + 2 * (size_t) N};
     RowSpace rs{n_local, nullptr, nullptr, cnt, scanned, entries, x, y, z};
     HydroSpace hs{h, u, vx, vy, vz, omega, P, cs};
     cudaStream_t s = (cudaStream_t) stream;
     // every staging entry the pair kernel reads is rewritten first: nothing to clear
     { k_stage_hydro<<<div_up(N, 256), 256, 0, s>>>(N, x, y, z, hs, pmass, b, b + 2 * (size_t) N); GBSPH_COUNTED; }
-    MixedParams p{(float) alpha_u, (float) alpha_AV, (float) beta_AV};
+    MixedParams p = mixed_params(pmass, alpha_u, alpha_AV, beta_AV);
     { k_derivs_mixed<<<div_up(n_local, 128), 128, 0, s>>>(rs, ms, p, pmass, ax, ay, az, du, vsig); GBSPH_COUNTED; }
     return cudaGetLastError() == cudaSuccess ? GBSPH_OK : GBSPH_ERR_CUDA;
 }

@@ -5,19 +5,20 @@
 
 namespace gbsph {
 
-// Rank-ordered FP32 staging of merged fields for the mixed pair kernels, five float4
-// (80 bytes) per particle in two records:
-//   position record P[2r], P[2r+1] (32 B, one sector):
-//     A = {x_hi, y_hi, z_hi, 1/h}      B = {x_lo, y_lo, z_lo, c_s}
-//   hydro record H[3r .. 3r+2] (48 B, two sectors):
-//     C = {vx_hi, vy_hi, vz_hi, u}     D = {vx_lo, vy_lo, vz_lo, rho}
-//     E = {P_hi, P_lo, 1/(rho^2 Omega), 1/(rho Omega)}
+// Rank-ordered FP32 staging of merged fields for the mixed pair kernels, two 32-byte
+// records per particle, each read with one 256-bit load:
+//   position record P[2r], P[2r+1]:
+//     {x_hi, y_hi, z_hi, 1/h}  {x_lo, y_lo, z_lo, c_s}
+//   hydro record H[2r], H[2r+1]:
+//     {vx_hi, vy_hi, vz_hi, u}  {P_hi, 1/(rho^2 Omega), bf16x2(vx_lo, vy_lo), bf16x2(vz_lo, P_lo)}
 // A position is carried as an unevaluated sum hi + lo of two floats (hi = fl32(x),
 // lo = fl32(x - hi)), so a pair separation (hi_a - hi_b) + (lo_a - lo_b) is accurate
 // to FP32 rounding of the separation itself, wherever the particles sit in the box.
+// Velocities and pressure keep their residuals as bfloat16 (about 2^-33 relative in
+// total); rho = m (hfact/h)^3 and 1/(rho Omega) are rebuilt from 1/h in the kernel.
 struct MixedSpace {
     const float4 *P; // 2 per particle
-    const float4 *H; // 3 per particle
+    const float4 *H; // 2 per particle
 };
 
 cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol);
