@@ -245,6 +245,30 @@ int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double
 int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
                       gbsph_time_state *ts, gbsph_step_log *log, void *stream);
 
+/* ------------------------------------------------------------------ adjoint */
+
+/* Cotangents (dL/d field) of one particle state, device arrays of n entries. */
+typedef struct {
+    uint32_t n;
+    uint32_t pad;
+    gbsph_vec3 gx, gv, ga; /* positions, velocities, accelerations */
+    double *gu, *gdu;      /* internal energy and its rate */
+} gbsph_cotangents;
+
+/* Reverse mode of one evolve_once (no reference counterpart: the differentiable step
+ * of the hot path).  `start` is the state the forward step began from (x, v, a, h, u,
+ * du; read only), t / dt / corrector_iters the forward step's time, dt and
+ * gbsph_step_log.corrector_iters.  The step is recomputed from `start` with the same
+ * dt and number of corrector evaluations (same tree, neighbour cache and ghosts), then
+ * reversed: on entry `cot` holds dL/d(state after the step), on return dL/d(state
+ * before it).  h after the step is treated as the exact solution of the density
+ * constraint; dt and the neighbour set are held fixed.  *g_alpha_av (host) is
+ * incremented by dL/d alpha_AV of this step.  FP64 reverse pass; the recompute runs in
+ * cfg->precision. */
+int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                       double t, double dt, uint32_t corrector_iters, gbsph_cotangents *cot,
+                       double *g_alpha_av, void *stream);
+
 /* ------------------------------------------------------------------ instrumentation
  * Per-stage device time measured with CUDA events on the launching stream (the role
  * of the reference's per-step timers, SolverStorage.hpp:111-118).  Enabling resets the

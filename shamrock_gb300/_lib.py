@@ -58,6 +58,11 @@ class StepLog(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Cotangents(C.Structure):
+    _fields_ = [("n", _u32), ("pad", _u32), ("gx", Vec3), ("gv", Vec3), ("ga", Vec3),
+                ("gu", _vp), ("gdu", _vp)]
+
+
 _P = C.POINTER
 SIGNATURES = {
     "gbsph_create": (C.c_int, [_P(_vp), C.c_int]),
@@ -90,6 +95,8 @@ SIGNATURES = {
     "gbsph_ghost_export": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbsph_evolve_once": (C.c_int, [_vp, _P(Particles), _P(Config), _P(TimeState), _P(StepLog),
                                     _vp]),
+    "gbsph_adjoint_step": (C.c_int, [_vp, _P(Particles), _P(Config), _f64, _f64, _u32,
+                                     _P(Cotangents), _P(_f64), _vp]),
     "gbsph_profile_kinds": (_u32, []),
     "gbsph_kernel_launches": (_u64, []),
     "gbsph_profile_name": (C.c_char_p, [_u32]),

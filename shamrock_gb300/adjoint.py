@@ -1,0 +1,192 @@
+"""Differentiable SPH rollout: a ``torch.autograd.Function`` over the C-ABI adjoint step.
+
+The reference has no adjoint; this is the differentiable form of its step
+(``Solver::evolve_once``, shammodels/sph/src/Solver.cpp:1942-3272) that the GB300 path adds.
+
+``rollout(model, v0, u0, alpha, n_steps, checkpoint_every, dts=None)`` runs ``n_steps``
+steps of ``model`` from its current positions, h, a and du with initial velocities
+``v0`` (3, N), internal energies ``u0`` (N,) and constant-AV ``alpha`` (alpha_AV), and
+returns the final ``(x, v, u)``.  Gradients flow to ``v0``, ``u0``, ``alpha`` and the
+initial positions ``x0`` when given.
+
+What is differentiated: the step map with each step's dt, its number of corrector
+evaluations and its neighbour cache held at the forward pass's values; h after each
+step is the exact root of the density constraint (implicit differentiation).  The
+forward pass records the dt sequence; pass it back as ``dts`` to replay the same map
+(e.g. for finite-difference checks), since the CFL dt itself is not differentiated.
+
+Memory: the state (x, v, a, h, u, du) is kept every ``checkpoint_every`` steps; the
+backward pass recomputes each segment from its checkpoint and reverses it step by step
+(``gbsph_adjoint_step`` recomputes the step once more on the device with its tape).
+"""
+
+import ctypes as C
+
+from . import _lib as L
+
+STATE_KEYS = ("xyz", "vxyz", "axyz", "hpart", "uint", "duint")
+
+
+def _snapshot(model):
+    d = model._to_device()
+    return {k: d[k].clone() for k in STATE_KEYS}
+
+
+def _restore(model, snap):
+    d = model._to_device()
+    for k in STATE_KEYS:
+        d[k].copy_(snap[k])
+
+
+def _particles_of(snap):
+    p = L.Particles()
+    p.n = snap["hpart"].shape[0]
+    for k in ("xyz", "vxyz", "axyz"):
+        t = snap[k]
+        setattr(p, k, L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0))
+    p.hpart = snap["hpart"].data_ptr()
+    p.uint = snap["uint"].data_ptr()
+    p.duint = snap["duint"].data_ptr()
+    p.omega = None
+    return p
+
+
+def _cot_struct(cot):
+    c = L.Cotangents()
+    c.n = cot["gu"].shape[0]
+    for name in ("gx", "gv", "ga"):
+        t = cot[name]
+        setattr(c, name, L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0))
+    c.gu = cot["gu"].data_ptr()
+    c.gdu = cot["gdu"].data_ptr()
+    return c
+
+
+def adjoint_step(model, start, t, dt, corrector_iters, cot):
+    """One reverse step (gbsph_adjoint_step): updates the cotangent dict ``cot`` in place
+    from d/d(state after) to d/d(state before) and returns dL/d alpha_AV of the step."""
+    import torch
+
+    lib = model._lib()
+    p = _particles_of(start)
+    cfg = model._config_struct()
+    cs = _cot_struct(cot)
+    g_alpha = C.c_double(0.0)
+    torch.cuda.synchronize()
+    lib.check(lib.lib.gbsph_adjoint_step(lib.handle, C.byref(p), C.byref(cfg), float(t),
+                                         float(dt), int(corrector_iters), C.byref(cs),
+                                         C.byref(g_alpha), None))
+    return g_alpha.value
+
+
+def _step(model, t, dt):
+    model.time = float(t)
+    model.dt = float(dt)
+    return model.evolve_once()
+
+
+class _Rollout:
+    """Forward bookkeeping shared by the autograd function and direct callers."""
+
+    def __init__(self, model, n_steps, checkpoint_every, dts=None):
+        self.model = model
+        self.n_steps = int(n_steps)
+        self.k = max(1, int(checkpoint_every))
+        self.dts = None if dts is None else [float(v) for v in dts]
+        self.records = []     # per step: (t, dt, corrector_iters)
+        self.checkpoints = {}  # step index -> state before that step
+
+    def forward(self):
+        m = self.model
+        t = m.time
+        for j in range(self.n_steps):
+            if j % self.k == 0:
+                self.checkpoints[j] = _snapshot(m)
+            dt = self.dts[j] if self.dts is not None else m.dt
+            log = _step(m, t, dt)
+            self.records.append((t, dt, int(log["corrector_iters"])))
+            t = t + dt
+            if self.dts is None:
+                m.dt = log["next_dt"]
+        return m
+
+    def backward(self, cot):
+        """cot: cotangents of the final state (dict gx, gv, ga, gu, gdu); updated in place
+        to the cotangents of the initial state.  Returns dL/d alpha_AV."""
+        import torch
+
+        m = self.model
+        saved = _snapshot(m)
+        saved_time = (m.time, m.dt, m.cfl_mult)
+        g_alpha = 0.0
+        starts = sorted(self.checkpoints)
+        for s0 in reversed(starts):
+            s1 = min(s0 + self.k, self.n_steps)
+            # states at the start of each step of the segment
+            _restore(m, self.checkpoints[s0])
+            seg = []
+            for j in range(s0, s1):
+                seg.append(_snapshot(m))
+                t, dt, _ = self.records[j]
+                if j + 1 < s1:
+                    _step(m, t, dt)
+            for j in reversed(range(s0, s1)):
+                t, dt, kk = self.records[j]
+                g_alpha += adjoint_step(m, seg[j - s0], t, dt, kk, cot)
+        _restore(m, saved)
+        m.time, m.dt, m.cfl_mult = saved_time
+        torch.cuda.synchronize()
+        return g_alpha
+
+
+def _zero_cot(n, dev):
+    import torch
+
+    z = lambda *s: torch.zeros(*s, dtype=torch.float64, device=dev)
+    return dict(gx=z(3, n), gv=z(3, n), ga=z(3, n), gu=z(n), gdu=z(n))
+
+
+def rollout(model, v0, u0, alpha, n_steps, checkpoint_every=5, dts=None, x0=None):
+    """Differentiable n-step rollout; returns (x_final, v_final, u_final) and records the
+    dt sequence in ``rollout.last_dts``."""
+    import torch
+
+    class Fn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, v0_, u0_, alpha_, x0_):
+            d = model._to_device()
+            if x0_ is not None:
+                d["xyz"].copy_(x0_)
+            d["vxyz"].copy_(v0_)
+            d["uint"].copy_(u0_)
+            model.cfg.av["alpha_AV"] = float(alpha_)
+            ro = _Rollout(model, n_steps, checkpoint_every, dts)
+            ro.forward()
+            ctx.ro = ro
+            ctx.has_x0 = x0_ is not None
+            rollout.last_dts = [r[1] for r in ro.records]
+            rollout.last_records = list(ro.records)
+            out = model._to_device()
+            return out["xyz"].clone(), out["vxyz"].clone(), out["uint"].clone()
+
+        @staticmethod
+        def backward(ctx, gx, gv, gu):
+            n = gu.shape[0] if gu is not None else model.get_total_part_count()
+            dev = model._to_device()["hpart"].device
+            cot = _zero_cot(n, dev)
+            if gx is not None:
+                cot["gx"].copy_(gx)
+            if gv is not None:
+                cot["gv"].copy_(gv)
+            if gu is not None:
+                cot["gu"].copy_(gu)
+            g_alpha = ctx.ro.backward(cot)
+            ga = torch.tensor(g_alpha, dtype=torch.float64)
+            return cot["gv"], cot["gu"], ga, (cot["gx"] if ctx.has_x0 else None)
+
+    alpha_t = alpha if isinstance(alpha, torch.Tensor) else torch.tensor(float(alpha), dtype=torch.float64)
+    return Fn.apply(v0, u0, alpha_t, x0)
+
+
+rollout.last_dts = None
+rollout.last_records = None

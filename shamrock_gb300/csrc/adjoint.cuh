@@ -1,0 +1,38 @@
+// Reverse-mode (adjoint) of one SPH step: declarations shared by adjoint.cu and the
+// step driver.
+#pragma once
+
+#include "sph_kernels.cuh"
+
+namespace gbsph {
+
+// Recorded by a forward step run for the adjoint: velocity and internal energy (SoA,
+// n each) before each corrector evaluation of the derivatives.
+struct StepTape {
+    u32 forced_iters = 0;   // run exactly this many corrector evaluations
+    u32 iters        = 0;   // evaluations recorded
+    DevBuf *snap     = nullptr;
+};
+constexpr u32 kTapeMaxIters = 16;
+
+struct AdjParams {
+    f64 pmass, gamma, alpha_u, alpha_AV, beta_AV, dt;
+};
+
+// Cotangents of one particle state (SoA), updated in place by adjoint_backward: on
+// entry with respect to the state after the step, on return with respect to the state
+// before it.
+struct CotState {
+    f64 *x[3], *v[3], *a[3];
+    f64 *u, *du;
+    u32 vs; // element stride of the vectors
+};
+
+// Runs the reverse pass of the step just recomputed in c (tree, cache, ghosts, the
+// converged h and Omega in h_local / omega_local, and the tape).  g_alpha accumulates
+// dL/d alpha_AV on the device.
+cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_local,
+                             const f64 *omega_local, const StepTape &tape, const AdjParams &p,
+                             const CotState &cot, f64 *g_alpha);
+
+} // namespace gbsph

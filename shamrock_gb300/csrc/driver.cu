@@ -3,6 +3,7 @@
 
 #include "../../include/gbsph.h"
 #include "gbsph_ctx.cuh"
+#include "adjoint.cuh"
 #include "sph_kernels.cuh"
 #include "sph_mixed.cuh"
 
@@ -63,7 +64,7 @@ Ctx::~Ctx() {
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
                       &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
-                      &dt_part};
+                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank};
     cudaSetDevice(device);
     for (DevBuf *b : bufs) b->release(stream);
     cudaStreamSynchronize(stream);
@@ -106,6 +107,39 @@ __global__ void k_reset_corrector(Scalars *sc) {
     sc->epsv2_max = 0;
     sc->dt_min    = ~0ull;
     sc->sum_v2    = 0;
+}
+
+// tape: velocity and energy (SoA) before a corrector evaluation
+__global__ void k_snap_vu(u32 n, const f64 *__restrict__ vx, const f64 *__restrict__ vy,
+                          const f64 *__restrict__ vz, u32 vs, const f64 *__restrict__ u,
+                          f64 *__restrict__ out) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t iv = (size_t) i * vs, n_ = n;
+    out[i]          = vx[iv];
+    out[n_ + i]     = vy[iv];
+    out[2 * n_ + i] = vz[iv];
+    out[3 * n_ + i] = u[i];
+}
+
+// working copy of a particle state (strided vectors -> SoA) for the adjoint recompute
+__global__ void k_copy_state(u32 n, gbsph_vec3 x, gbsph_vec3 v, gbsph_vec3 a, const f64 *h,
+                             const f64 *u, const f64 *du, f64 *__restrict__ out) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t n_ = n;
+    out[0 * n_ + i]  = x.x[(size_t) i * x.stride];
+    out[1 * n_ + i]  = x.y[(size_t) i * x.stride];
+    out[2 * n_ + i]  = x.z[(size_t) i * x.stride];
+    out[3 * n_ + i]  = v.x[(size_t) i * v.stride];
+    out[4 * n_ + i]  = v.y[(size_t) i * v.stride];
+    out[5 * n_ + i]  = v.z[(size_t) i * v.stride];
+    out[6 * n_ + i]  = a.x[(size_t) i * a.stride];
+    out[7 * n_ + i]  = a.y[(size_t) i * a.stride];
+    out[8 * n_ + i]  = a.z[(size_t) i * a.stride];
+    out[9 * n_ + i]  = h[i];
+    out[10 * n_ + i] = u[i];
+    out[11 * n_ + i] = du[i];
 }
 
 } // namespace
@@ -459,9 +493,12 @@ int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double
     return GBSPH_OK;
 }
 
-int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
-                      gbsph_time_state *ts, gbsph_step_log *log, void *stream) {
-    ENTER(ctx, stream);
+} // extern "C"
+
+// One step (Solver::evolve_once).  With a tape, exactly tape->forced_iters corrector
+// evaluations run and the velocity / energy before each is recorded.
+static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
+                       gbsph_time_state *ts, gbsph_step_log *log, StepTape *tape) {
     Ctx &c = ctx->c;
     REQUIRE_ARG(p && cfg && ts, "null argument");
     REQUIRE_ARG(p->n > 0, "empty patch");
@@ -578,6 +615,10 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
     // ---- corrector loop (Solver.cpp:2247-3171)
     DevBuf *rank_bufs[] = {&c.sh2, &c.su, &c.svx, &c.svy, &c.svz, &c.som, &c.sP, &c.scs};
     for (DevBuf *b : rank_bufs) CU(b->ensure(8 * (size_t) N, s));
+    if (tape) {
+        CU(tape->snap->ensure(sizeof(f64) * 4 * (size_t) n * tape->forced_iters, s));
+        tape->iters = 0;
+    }
     HydroSpace hs{c.sh2.as<f64>(), c.su.as<f64>(),  c.svx.as<f64>(), c.svy.as<f64>(),
                   c.svz.as<f64>(), c.som.as<f64>(), c.sP.as<f64>(),  c.scs.as<f64>()};
     f64 next_cfl   = 0;
@@ -589,6 +630,12 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
                         "the corrector has made over 50 loops, either their is a bug, either you "
                         "are using a dt that is too large");
         CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, cfg->gamma));
+        if (tape) {
+            { k_snap_vu<<<div_up(n, 256), 256, 0, s>>>(
+                n, lf.vx, lf.vy, lf.vz, lf.vs, lf.u,
+                tape->snap->as<f64>() + (size_t) corr_iters * 4 * n); GBSPH_COUNTED; }
+            tape->iters = corr_iters + 1;
+        }
         { k_reset_corrector<<<1, 1, 0, s>>>(dsc); GBSPH_COUNTED; }
         f64 C_cour  = cfg->cfl_cour * ts->cfl_mult;
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
@@ -604,7 +651,10 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
         f64 eps_v       = rank_veps_v / vmean;
         if (vmean <= 0) eps_v = 0;
         lg.eps_v = eps_v;
-        if (eps_v > 1e-2) {
+        if (tape) {
+            rerun    = corr_iters + 1 < tape->forced_iters;
+            next_cfl = ordered_to_f64(c.h_scalars->dt_min);
+        } else if (eps_v > 1e-2) {
             rerun        = true;
             ts->cfl_mult = ts->cfl_mult / 2;
         } else {
@@ -630,6 +680,69 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
     if (log) *log = lg;
     if (!converged) ctx->c.err = "the h iterator is not converged after the maximum number of "
                                  "sub-cycles (step continued, as the reference does)";
+    return GBSPH_OK;
+}
+
+extern "C" {
+
+int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
+                      gbsph_time_state *ts, gbsph_step_log *log, void *stream) {
+    ENTER(ctx, stream);
+    return evolve_impl(ctx, p, cfg, ts, log, nullptr);
+}
+
+int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                       double t, double dt, uint32_t corrector_iters, gbsph_cotangents *cot,
+                       double *g_alpha_av, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(start && cfg && cot, "null argument");
+    REQUIRE_ARG(start->n > 0 && cot->n == start->n, "cotangents and state differ in size");
+    REQUIRE_ARG(corrector_iters >= 1 && corrector_iters <= kTapeMaxIters,
+                "corrector_iters must be the forward step's count (1..16)");
+    REQUIRE_ARG(cot->gx.stride == cot->gv.stride && cot->gx.stride == cot->ga.stride,
+                "gx, gv and ga must share one element stride");
+    REQUIRE_ARG(dt >= 0, "dt must be the forward step's dt");
+    cudaStream_t s = c.stream;
+    const u32 n    = start->n;
+    // recompute the step on a working copy of the start state
+    CU(c.adj_state.ensure(sizeof(f64) * 12 * (size_t) n, s));
+    f64 *W = c.adj_state.as<f64>();
+    size_t n_ = n;
+    { k_copy_state<<<div_up(n, 256), 256, 0, s>>>(n, start->xyz, start->vxyz, start->axyz,
+                                                start->hpart, start->uint, start->duint, W); GBSPH_COUNTED; }
+    CU(cudaGetLastError());
+    gbsph_particles w;
+    std::memset(&w, 0, sizeof(w));
+    w.n     = n;
+    w.xyz   = gbsph_vec3{W, W + n_, W + 2 * n_, 1, 0};
+    w.vxyz  = gbsph_vec3{W + 3 * n_, W + 4 * n_, W + 5 * n_, 1, 0};
+    w.axyz  = gbsph_vec3{W + 6 * n_, W + 7 * n_, W + 8 * n_, 1, 0};
+    w.hpart = W + 9 * n_;
+    w.uint  = W + 10 * n_;
+    w.duint = W + 11 * n_;
+    gbsph_time_state ts{t, dt, 1.0};
+    StepTape tape;
+    tape.forced_iters = corrector_iters;
+    tape.snap         = &c.adj_snap;
+    int st = evolve_impl(ctx, &w, cfg, &ts, nullptr, &tape);
+    if (st != GBSPH_OK) return st;
+    RowSpace rs{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
+                c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
+                c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
+    AdjParams ap{cfg->pmass, cfg->gamma, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV, dt};
+    CotState cs;
+    cs.x[0] = cot->gx.x; cs.x[1] = cot->gx.y; cs.x[2] = cot->gx.z;
+    cs.v[0] = cot->gv.x; cs.v[1] = cot->gv.y; cs.v[2] = cot->gv.z;
+    cs.a[0] = cot->ga.x; cs.a[1] = cot->ga.y; cs.a[2] = cot->ga.z;
+    cs.u    = cot->gu;
+    cs.du   = cot->gdu;
+    cs.vs   = cot->gx.stride;
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    CU(cudaMemsetAsync(&dsc->g_alpha, 0, sizeof(f64), s));
+    CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), tape, ap, cs, &dsc->g_alpha));
+    CU(sync_scalars(c));
+    if (g_alpha_av) *g_alpha_av += c.h_scalars->g_alpha;
     return GBSPH_OK;
 }
 

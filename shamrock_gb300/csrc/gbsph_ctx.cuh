@@ -30,6 +30,7 @@ struct Scalars {
     u64 n_unconverged; // particles whose per-thread iteration cap was hit
     u64 csr_entries;   // stage-2 entries of the one-pass cache build
     f64 sum_v2;        // sum of |v|^2 after the corrector
+    f64 g_alpha;       // adjoint: dL / d alpha_AV of one step
     f64 cons[8];       // conservation totals (momentum, energies)
     u32 total;         // scan totals
     u32 total2;
@@ -131,6 +132,9 @@ struct Ctx {
     // ---- per-row / per-local work arrays
     DevBuf h_old_row, eps_row, omega_local, a_old, du_old, hnew_row, omega_row;
     DevBuf dt_part;
+
+    // ---- adjoint: working state, tape, accumulators (local and rank order)
+    DevBuf adj_state, adj_snap, adj_loc, adj_rank;
 
     ~Ctx();
 };
