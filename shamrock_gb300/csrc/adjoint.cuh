@@ -30,9 +30,9 @@ struct CotState {
 
 // Runs the reverse pass of the step just recomputed in c (tree, cache, ghosts, the
 // converged h and Omega in h_local / omega_local, and the tape).  g_alpha accumulates
-// dL/d alpha_AV on the device.
+// dL/d alpha_AV on the device.  fp32: FP32 pair arithmetic (else FP64).
 cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_local,
                              const f64 *omega_local, const StepTape &tape, const AdjParams &p,
-                             const CotState &cot, f64 *g_alpha);
+                             const CotState &cot, f64 *g_alpha, bool fp32);
 
 } // namespace gbsph

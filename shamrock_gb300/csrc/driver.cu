@@ -740,7 +740,8 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     cs.vs   = cot->gx.stride;
     Scalars *dsc = c.d_scalars.as<Scalars>();
     CU(cudaMemsetAsync(&dsc->g_alpha, 0, sizeof(f64), s));
-    CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), tape, ap, cs, &dsc->g_alpha));
+    CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), tape, ap, cs, &dsc->g_alpha,
+                        cfg->precision == GBSPH_MIXED));
     CU(sync_scalars(c));
     if (g_alpha_av) *g_alpha_av += c.h_scalars->g_alpha;
     return GBSPH_OK;
