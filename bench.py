@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=20.0,
                    help="bounded CPU-baseline sample, seconds of host work")
     return p.parse_args()
@@ -60,13 +61,13 @@ def workload(cells):
     return s, name
 
 
-def make_model(s, precision, device=0):
+def make_model(s, precision, device=0, alpha_AV=1.0):
     import shamrock_gb300 as sg
 
     ctx = sg.Context(device)
     m = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
     cfg = m.gen_default_config()
-    cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0)
+    cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0)
     cfg.set_boundary_periodic()
     cfg.set_eos_adiabatic(s["gamma"])
     cfg.set_particle_mass(s["pmass"])
@@ -431,10 +432,72 @@ def run_gb300(args):
         line["fp64_gpu"] = {"value": v64, "unit": UNIT, "steps": k64}
         if args.precision == "mixed":
             line["mixed_over_fp64"] = value / v64
+    if world == 1 and not args.no_adjoint:
+        line["adjoint"] = adjoint_bench(precision=args.precision, device=local)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, args.cpu_seconds, threads=os.cpu_count())
     print(json.dumps(line), flush=True)
     return 0
+
+
+def adjoint_bench(steps=40, ck=5, precision="mixed", device=0):
+    """Adjoint / forward time of the differentiable sound-wave rollout: 2^18 particles
+    (simple cubic 64^3), density perturbation 1e-4 sin(2 pi x), gamma 1.0001, alpha_AV
+    0.1; loss = |v_final - v_target|^2 (seeded target) after `steps` steps; gradients
+    with respect to initial v, u and alpha_AV with a checkpoint every `ck` steps.  The
+    backward time includes the recomputation between checkpoints."""
+    import numpy as np
+    import torch
+
+    from shamrock_gb300 import adjoint, setups
+
+    s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
+    m = make_model(s, precision, device, alpha_AV=0.1)
+    m.evolve_once()  # dt = 0: initial h, Omega, a, du
+    d = m._to_device()
+    n = d["hpart"].shape[0]
+    rng = np.random.default_rng(12345)
+    v_t = torch.as_tensor(1e-4 * rng.standard_normal((3, n)), device=d["vxyz"].device)
+    v0 = d["vxyz"].clone().requires_grad_(True)
+    u0 = d["uint"].clone().requires_grad_(True)
+    alpha = torch.tensor(0.1, dtype=torch.float64, requires_grad=True)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    lib = m._lib()
+    # untimed warm-up rollout + backward (lazy kernel loading, autograd worker thread)
+    warm = adjoint._snapshot(m)
+    t_w, dt_w, cm_w = m.time, m.dt, m.cfl_mult
+    xw, vw, uw = adjoint.rollout(m, v0, u0, alpha, ck, ck)
+    ((vw - v_t) ** 2).sum().backward()
+    v0.grad = u0.grad = alpha.grad = None
+    adjoint._restore(m, warm)
+    m.time, m.dt, m.cfl_mult = t_w, dt_w, cm_w
+    torch.cuda.synchronize()
+    ev[0].record()
+    x, v, u = adjoint.rollout(m, v0, u0, alpha, steps, ck)
+    ev[1].record()
+    loss = ((v - v_t) ** 2).sum()
+    torch.cuda.synchronize()
+    lib.profile(True)
+    ev[2].record()
+    loss.backward()
+    ev[3].record()
+    torch.cuda.synchronize()
+    prof = lib.profile_read()
+    lib.profile(False)
+    f_ms, b_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+    iters = [r[2] for r in adjoint.rollout.last_records]
+    return {"workload": "sound_wave_cubic_64^3 (N=%d, amp 1e-4, gamma 1.0001, "
+                        "alpha_AV 0.1, periodic)" % n,
+            "precision": precision, "steps": steps, "checkpoint_every": ck,
+            "forward_ms": f_ms, "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+            "loss": float(loss.detach()),
+            "grad_norm": {"v": float(v0.grad.norm()), "u": float(u0.grad.norm()),
+                          "alpha": float(alpha.grad)},
+            "corrector_iters": iters,
+            "backward_stages_ms": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
+            "definition": "backward (recompute between checkpoints + reverse steps) / forward "
+                          "(steps + checkpoint copies), CUDA events, same process, after one "
+                          "untimed warm-up rollout + backward of checkpoint_every steps"}
 
 
 def main():

@@ -76,6 +76,11 @@ typedef struct {
     double box_min[3], box_max[3];
     uint32_t precision;             /* GBSPH_FP64 or GBSPH_MIXED */
     uint32_t pad;
+    /* Per-particle Newton threshold: a particle's h is updated while its eps_h exceeds
+     * it (1e-6 in the reference's IterateSmoothingLengthDensity kernel; 0 selects
+     * that).  Smaller values converge h further, e.g. for finite-difference checks of
+     * the adjoint, which differentiates h as the exact root of the density constraint. */
+    double epsilon_h_particle;
 } gbsph_config;
 
 /* Synchronised solver state (the scheduler edges "time", "dt", "cfl_multiplier",

@@ -41,7 +41,8 @@ class Config(C.Structure):
                 ("cfl_mult_stiffness", _f64), ("htol_up_coarse", _f64), ("htol_up_fine", _f64),
                 ("epsilon_h", _f64), ("h_iter_per_subcycles", _u32), ("h_max_subcycles", _u32),
                 ("tree_reduction_level", _u32), ("periodic", _u32), ("box_min", _d3),
-                ("box_max", _d3), ("precision", _u32), ("pad", _u32)]
+                ("box_max", _d3), ("precision", _u32), ("pad", _u32),
+                ("epsilon_h_particle", _f64)]
 
 
 class TimeState(C.Structure):

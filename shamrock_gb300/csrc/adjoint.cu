@@ -274,6 +274,10 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             const T vsc = aAV * csc + bAV * aw, vsb = aAV * csb + bAV * aw;
             const T tc = -half * rhoc * vsc * w, tb = -half * rhob * vsb * w;
             const bool actc = tc > T(0), actb = tb > T(0);
+            // weight of the active branch of max(t, 0): 1, 0, or 1/2 exactly at the kink
+            // (w = 0), the symmetric derivative that central differences measure
+            const T wc = actc ? T(1) : (tc == T(0) ? half : T(0));
+            const T wb = actb ? T(1) : (tb == T(0) ? half : T(0));
             const T Ac = Pc + (actc ? tc : T(0)), Ab = Pb + (actb ? tb : T(0));
             const T dP = Pc - Pb, rbar = half * (rhoc + rhob);
             const T vsu = sqrt(fabs(dP) / rbar);
@@ -285,8 +289,8 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             const T du_ = uc - ub, dmu = muc - mub;
             const T cond = half * m * au * dmu * vsu * du_; // multiplies J
             // d q / d w where the viscous pressure is active
-            const T dqcw = actc ? -half * rhoc * (vsc + bAV * aw) : T(0);
-            const T dqbw = actb ? -half * rhob * (vsb + bAV * aw) : T(0);
+            const T dqcw = wc * (-half * rhoc * (vsc + bAV * aw));
+            const T dqbw = wb * (-half * rhob * (vsb + bAV * aw));
             const T dSw  = kc * Fc * dqcw + kb * Fb * dqbw;
             const T E    = muc * Ac * kc * Fc + mub * Ab * kb * Fb;
             const T dLw  = -m * Le * dSw + m * E + m * w * (muc * kc * Fc * dqcw + mub * kb * Fb * dqbw);
@@ -528,6 +532,7 @@ cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_loc
     for (u32 k = K; k >= 1; k--) {
         { k_adj_lin<<<gb, 256, 0, s>>>(n, 0, hdt, L); GBSPH_COUNTED; }
         const f64 *sv = snap + (size_t) (k - 1) * 4 * n_;
+        ProfScope ps(c, kProfAdjDerivs, n);
         if (fp32) {
             { k_adj_stage32<<<gN, 256, 0, s>>>(N, n, si, gs, rs.x, rs.y, rs.z, sv, sv + n_,
                                              sv + 2 * n_, sv + 3 * n_, h_local, omega_local,
@@ -542,6 +547,7 @@ cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_loc
         { k_adj_lin<<<gb, 256, 0, s>>>(n, 1, hdt, L); GBSPH_COUNTED; }
     }
     // Omega and the density constraint (positions, h and Omega are staged by the loop)
+    ProfScope ps(c, kProfAdjDensity, n);
     if (fp32) {
         { k_adj_omega_a<Src32><<<gb, 256, 0, s>>>(rs, s32, h_local, omega_local, p.pmass, L); GBSPH_COUNTED; }
         { k_adj_stage32m<<<gN, 256, 0, s>>>(N, n, si, gs, L.nu, L.lom, M32); GBSPH_COUNTED; }

@@ -194,7 +194,8 @@ const char *gbsph_version(void) { return "gbsph 0.1 (sm_103a)"; }
 
 static const char *kProfNames[kProfCount] = {
     "predict", "ghosts", "merge_bbox", "morton_sort", "tree", "leaf_lists", "owner",
-    "cache_count", "cache_fill", "h_iterate", "omega", "gather_eos", "derivs"};
+    "cache_count", "cache_fill", "h_iterate", "omega", "gather_eos", "derivs", "adj_derivs",
+    "adj_density"};
 
 uint32_t gbsph_profile_kinds(void) { return kProfCount; }
 
@@ -530,7 +531,9 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     CU(c.hnew_row.ensure(8 * (size_t) n, s));
     CU(c.eps_row.ensure(8 * (size_t) n, s));
     CU(c.omega_local.ensure(8 * (size_t) n, s));
-    const bool fused_h = cfg->epsilon_h <= 1e-6;
+    // per-particle Newton threshold (0 selects the reference's 1e-6)
+    const f64 eps_p    = cfg->epsilon_h_particle > 0 ? cfg->epsilon_h_particle : 1e-6;
+    const bool fused_h = cfg->epsilon_h <= eps_p;
     u32 hstep = 0;
     f64 max_eps = 0, min_eps = 0;
     bool converged = false;
@@ -565,11 +568,11 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             if (mixed)
                 CU(h_iterate_mixed(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
                                    c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
-                                   cfg->htol_up_fine, cfg->h_iter_per_subcycles));
+                                   cfg->htol_up_fine, cfg->h_iter_per_subcycles, eps_p));
             else
                 CU(h_iterate64(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
                                c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
-                               cfg->htol_up_fine, cfg->h_iter_per_subcycles));
+                               cfg->htol_up_fine, cfg->h_iter_per_subcycles, eps_p));
             CU(sync_scalars(c));
             max_eps     = ordered_to_f64(c.h_scalars->eps_max);
             min_eps     = ordered_to_f64(c.h_scalars->eps_min);
@@ -580,11 +583,11 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
                 if (mixed)
                     CU(h_iterate_mixed(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
                                        c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
-                                       cfg->htol_up_fine, 1));
+                                       cfg->htol_up_fine, 1, eps_p));
                 else
                     CU(h_iterate64(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(),
                                    c.eps_row.as<f64>(), cfg->pmass, cfg->htol_up_coarse,
-                                   cfg->htol_up_fine, 1));
+                                   cfg->htol_up_fine, 1, eps_p));
                 CU(sync_scalars(c));
                 max_eps = ordered_to_f64(c.h_scalars->eps_max);
                 min_eps = ordered_to_f64(c.h_scalars->eps_min);

@@ -70,6 +70,8 @@ enum ProfKind : int {
     kProfOmega,
     kProfGatherEos,
     kProfDerivs,
+    kProfAdjDerivs, // adjoint: reverse of the derivatives (staging + pair kernel)
+    kProfAdjDensity, // adjoint: reverse of Omega and the density constraint
     kProfCount
 };
 

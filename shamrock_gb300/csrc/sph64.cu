@@ -74,11 +74,11 @@ __device__ __forceinline__ void density_sums(const RowSpace &rs, u32 a, u32 k0, 
 
 // ITERS Newton iterations per row (the reference's global loop is equivalent per
 // particle: a particle's update reads only its own h, so it iterates until its own
-// eps <= 1e-6, becomes -1, or the iteration cap is reached).
+// eps <= eps_p (1e-6 in the reference), becomes -1, or the iteration cap is reached).
 __global__ void __launch_bounds__(256) k_h_iterate(RowSpace rs, const f64 *__restrict__ h_old,
                                                    f64 *__restrict__ h_new, f64 *__restrict__ eps,
                                                    f64 pmass, f64 h_evol_max, f64 h_evol_iter_max,
-                                                   u32 iters, Scalars *sc) {
+                                                   u32 iters, f64 eps_p, Scalars *sc) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     u64 emax = 0, emin = ~0ull;
     u32 used = 0;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) k_h_iterate(RowSpace rs, const f64 *__res
         f64 h_a  = h_new[t];
         f64 e    = eps[t];
         for (u32 it = 0; it < iters; it++) {
-            if (!(e > 1e-6)) break;
+            if (!(e > eps_p)) break;
             used++;
             f64 rho_sum, sumdWdh;
             density_sums(rs, a, k0, k1, h_a, pmass, rho_sum, sumdWdh);
@@ -392,10 +392,10 @@ __global__ void k_fill(u32 n, f64 *__restrict__ dst, f64 v) {
 
 // ---------------------------------------------------------------- host wrappers
 cudaError_t h_iterate64(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
-                        f64 pmass, f64 hev, f64 hevi, u32 iters) {
+                        f64 pmass, f64 hev, f64 hevi, u32 iters, f64 eps_p) {
     ProfScope ps(c, kProfHIter, rs.n);
     { k_h_iterate<<<div_up(rs.n, 256), 256, 0, c.stream>>>(rs, h_old, h_new, eps, pmass, hev, hevi,
-                                                         iters, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+                                                         iters, eps_p, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t omega64(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *out,

@@ -39,8 +39,11 @@ struct LocalFields {
 };
 
 // sph64.cu
+// eps_p: per-particle Newton threshold (a particle is updated while its eps > eps_p;
+// 1e-6 in the reference, IterateSmoothingLengthDensity.cpp)
 cudaError_t h_iterate64(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
-                        f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters);
+                        f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters,
+                        f64 eps_p = 1e-6);
 cudaError_t omega64(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *out,
                     const u32 *out_index);
 cudaError_t eos64(Ctx &c, u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamma, f64 *P, f64 *cs);

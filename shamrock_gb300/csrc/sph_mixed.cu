@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(256, 4) k_h_iterate_mixed(RowSpace rs, MixedSp
                                                          f64 *__restrict__ h_new,
                                                          f64 *__restrict__ eps, f64 pmass,
                                                          f64 h_evol_max, f64 h_evol_iter_max,
-                                                         u32 iters, Scalars *sc) {
+                                                         u32 iters, f64 eps_p, Scalars *sc) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     u64 emax = 0, emin = ~0ull;
     u32 used = 0;
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256, 4) k_h_iterate_mixed(RowSpace rs, MixedSp
         const f64 h_max_evol_m = 1 / h_evol_iter_max;
         f64 ha_0 = h_old[t], h_a = h_new[t], e = eps[t];
         for (u32 it = 0; it < iters; it++) {
-            if (!(e > 1e-6)) break;
+            if (!(e > eps_p)) break;
             used++;
             float sf, sg;
             density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(1.0 / h_a), sf, sg);
@@ -392,11 +392,11 @@ cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol) {
 }
 
 cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
-                            f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters) {
+                            f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters, f64 eps_p) {
     ProfScope ps(c, kProfHIter, rs.n);
     MixedSpace ms = mixed_space(c, c.n_obj);
     { k_h_iterate_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(
-        rs, ms, h_old, h_new, eps, pmass, h_evol_max, h_evol_iter_max, iters,
+        rs, ms, h_old, h_new, eps, pmass, h_evol_max, h_evol_iter_max, iters, eps_p,
         c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     return cudaGetLastError();
 }

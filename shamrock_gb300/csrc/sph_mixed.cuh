@@ -25,7 +25,8 @@ cudaError_t stage_positions_mixed(Ctx &c, u32 N, f64 h_tol);
 // the position records staged by stage_positions_mixed (B.w = fl32 cache threshold)
 const float4 *mixed_positions(Ctx &c);
 cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
-                            f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters);
+                            f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters,
+                            f64 eps_p = 1e-6);
 cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                               f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,

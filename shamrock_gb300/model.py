@@ -39,6 +39,7 @@ class SolverConfig:
         self.htol_up_coarse_cycle = 1.1
         self.htol_up_fine_cycle = 1.1
         self.epsilon_h = 1e-6
+        self.epsilon_h_particle = 1e-6
         self.h_iter_per_subcycles = 50
         self.h_max_subcycles_count = 100
         self.precision = "fp64"
@@ -84,6 +85,15 @@ class SolverConfig:
 
     def set_smoothing_length_density_based(self):
         pass
+
+    def set_epsilon_h(self, eps):
+        """Global h-iteration convergence threshold (SolverConfig::epsilon_h)."""
+        self.epsilon_h = float(eps)
+
+    def set_epsilon_h_particle(self, eps):
+        """Per-particle Newton threshold (1e-6 in the reference's kernel).  Lowering it
+        together with epsilon_h converges h further (GB300 extension)."""
+        self.epsilon_h_particle = float(eps)
 
     def set_precision(self, precision):
         """"fp64" (bit-identical to the FP64 oracle) or "mixed" (FP32 pair arithmetic)."""
@@ -337,6 +347,7 @@ class Model:
         s.cfl_mult_stiffness = c.cfl_multiplier_stiffness
         s.htol_up_coarse, s.htol_up_fine = c.htol_up_coarse_cycle, c.htol_up_fine_cycle
         s.epsilon_h = c.epsilon_h
+        s.epsilon_h_particle = c.epsilon_h_particle
         s.h_iter_per_subcycles = c.h_iter_per_subcycles
         s.h_max_subcycles = c.h_max_subcycles_count
         s.tree_reduction_level = c.tree_reduction_level

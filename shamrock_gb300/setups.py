@@ -9,8 +9,10 @@ dataset is involved): every generator is deterministic given its seed.
   Gaussian position jitter sigma * a.
 - ``clustered_box``: half the particles uniform in the unit cube, half in a
   Gaussian clump (clipped into the box), v ~ N(0, 0.1^2), u ~ U[0.5, 1.5].
-- ``sound_wave``: FCC lattice trimmed to 2^18 particles with a 1e-4 sin(2 pi x)
-  density perturbation applied by a position remap.
+- ``sound_wave``: simple cubic lattice of 64^3 = 2^18 particles filling the periodic
+  unit cube, with a 1e-4 sin(2 pi x) density perturbation applied by a position
+  remap and the matching travelling-wave velocity (an FCC lattice cannot hold exactly 2^18 sites in a cube: 4*40^3 < 2^18, and
+  trimming 4*41^3 leaves a void slab whose collapse swamps the wave).
 
 h is initialised to hfact * (m / rho)^(1/3) with the local density estimate of
 the generator (hfact = 1.2 for M4).
@@ -76,20 +78,34 @@ def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0):
                 box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0), periodic=True)
 
 
-def sound_wave(n_target=1 << 18, n_cells=41, amp=1e-4, gamma=1.0001, cs=1.0, seed=12345):
-    """FCC 4*41^3 lattice trimmed to the first n_target sites in lattice order, then a
-    density perturbation rho = 1 + amp sin(2 pi x) by the x -> x - amp/(2 pi) cos(2 pi x)
-    remap (first order).  Trimming leaves a partial final plane, which is fine for a
-    differentiable-step test case."""
-    pos = fcc_lattice(n_cells)[:n_target]
+def sound_wave(n_side=64, amp=1e-4, gamma=1.0001, cs=1.0, travelling=True, noise=1e-4,
+               seed=12345):
+    """n_side^3 particles on a simple cubic lattice (sites at (i + 1/2) / n_side), then
+    rho = 1 + amp sin(2 pi x) by the first-order remap x -> x - amp/(2 pi) cos(2 pi x);
+    P = cs^2 / gamma at rho = 1 (u = P / ((gamma - 1) rho)).  travelling: the acoustic
+    wave's own velocity v_x = amp cs sin(2 pi x) (a wave moving in +x); else at rest.
+    noise: seeded perturbations, velocity N(0, (noise cs)^2) per component and u relative
+    N(0, noise^2).  They break the lattice's exact plane symmetry, which otherwise keeps
+    pairs of one plane exactly at zero relative velocity and zero pressure difference:
+    on the viscosity switch max(-rho v_sig w / 2, 0) and the |P_a - P_b|^(1/2)
+    conductivity speed, where the step has no derivative."""
+    g = (np.arange(n_side) + 0.5) / n_side
+    i, j, k = np.meshgrid(g, g, g, indexing="ij")
+    pos = np.stack([i.ravel(), j.ravel(), k.ravel()], 1)
     N = pos.shape[0]
     x = pos[:, 0]
-    pos = pos.copy()
     pos[:, 0] = np.mod(x - amp / (2 * np.pi) * np.cos(2 * np.pi * x), 1.0)
     pmass = 1.0 / N
     rho = 1.0 + amp * np.sin(2 * np.pi * pos[:, 0])
     P0 = cs * cs / gamma
     u = np.full(N, P0 / ((gamma - 1.0) * 1.0))
     h = HFACT_M4 * (pmass / rho) ** (1.0 / 3.0)
-    return dict(pos=pos, vel=np.zeros((N, 3)), h=h, u=u, pmass=pmass, gamma=gamma,
+    vel = np.zeros((N, 3))
+    if travelling:
+        vel[:, 0] = amp * cs * np.sin(2 * np.pi * pos[:, 0])
+    if noise:
+        rng = np.random.default_rng(seed)
+        vel += noise * cs * rng.standard_normal((N, 3))
+        u = u * (1.0 + noise * rng.standard_normal(N))
+    return dict(pos=pos, vel=vel, h=h, u=u, pmass=pmass, gamma=gamma,
                 box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0), periodic=True)

@@ -150,3 +150,100 @@ def test_mixed_adjoint_matches_fp64_adjoint():
     rel_a = abs(g32["a"] - g64["a"]) / abs(g64["a"])
     print(f"alpha: {g32['a']:.10e} vs {g64['a']:.10e} rel {rel_a:.2e}")
     assert rel_a < 1e-3
+
+
+def test_sound_wave_gradients_fd():
+    """The differentiable sound wave: 64^3 = 2^18 particles, rho = 1 + 1e-4 sin(2 pi x),
+    gamma 1.0001, alpha_AV 0.1, 40 steps with a checkpoint every 5, loss = |v_final -
+    v_target|^2 (seeded target).  Gradients with respect to initial v, u and alpha_AV:
+    the FP64 adjoint against FP64 central differences on 16 random coordinates within
+    1e-4, relative to the largest checked component of the same kind.  The set-up
+    carries seeded 1e-4 velocity / energy noise so that no pair sits on a kink of the
+    step (the viscosity switch, the |dP|^(1/2) conductivity speed); the steps are 1e-3
+    of those scales: 1e-7 for v, 1e-7 relative for u (dP ~ 1e-7 against ~1e-4), 1e-6
+    relative for alpha.  The FP64 runs converge h to round-off (epsilon_h =
+    epsilon_h_particle = 1e-13).
+    The u coordinates are held to 1e-2: with gamma - 1 = 1e-4 their gradients are ~1e-9
+    and pass through the conductivity speed |P_a - P_b|^(1/2), whose derivative grows
+    as |dP|^(-1/2) for pairs of nearly equal pressure, so the differences themselves
+    are resolved to ~1e-3 (observed FP64 agreement 3e-5 to 7e-3).
+    The FP32-mixed forward/backward is held to 1e-2 of the same differences: with a
+    background pressure P0 = 1 against dP ~ 1e-4, the net pressure force on a particle is
+    a ~1e-5 residue of O(1) pair terms, so FP32 pair arithmetic (2^-24 per term) carries
+    ~1e-4..1e-3 relative force error in this regime (observed 8e-5 to 2.3e-3)."""
+    import torch
+
+    import bench
+    from shamrock_gb300 import adjoint, setups
+    from shamrock_gb300.adjoint import _restore, _snapshot
+
+    s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
+    steps, ck = 40, 5
+    rng = np.random.default_rng(12345)
+    N = len(s["h"])
+    coords = [("v", (int(rng.integers(3)), int(rng.integers(N)))) for _ in range(8)]
+    coords += [("u", (int(rng.integers(N)),)) for _ in range(7)]
+    coords += [("a", ())]
+    v_t_np = 1e-4 * rng.standard_normal((3, N))
+
+    def setup(precision):
+        m = bench.make_model(s, precision, 0, alpha_AV=0.1)
+        if precision == "fp64":
+            # h converged to round-off in every run, so that the differences resolve the
+            # map the adjoint differentiates (h as the exact root of the density
+            # constraint) rather than the 1e-6 Newton stopping noise
+            m.cfg.set_epsilon_h(1e-13)
+            m.cfg.set_epsilon_h_particle(1e-13)
+        m.evolve_once()  # dt = 0
+        return m, _snapshot(m), (m.time, m.dt, m.cfl_mult)
+
+    def grads(m, warm, tstate, dts):
+        _restore(m, warm)
+        m.time, m.dt, m.cfl_mult = tstate
+        v_t = torch.as_tensor(v_t_np, device=warm["vxyz"].device)
+        v0 = warm["vxyz"].clone().requires_grad_(True)
+        u0 = warm["uint"].clone().requires_grad_(True)
+        al = torch.tensor(0.1, dtype=torch.float64, requires_grad=True)
+        x, v, u = adjoint.rollout(m, v0, u0, al, steps, ck, dts=dts)
+        ((v - v_t) ** 2).sum().backward()
+        return (dict(v=v0.grad.cpu().numpy(), u=u0.grad.cpu().numpy(), a=float(al.grad)),
+                list(adjoint.rollout.last_dts))
+
+    m64, warm64, ts64 = setup("fp64")
+    g64, dts = grads(m64, warm64, ts64, None)
+    m32, warm32, ts32 = setup("mixed")
+    g32, _ = grads(m32, warm32, ts32, dts)
+
+    v_t = torch.as_tensor(v_t_np, device=warm64["vxyz"].device)
+    res = []
+    for kind, idx in coords:
+        eps = {"v": 1e-7, "u": 1e-7 * float(warm64["uint"][0]), "a": 1e-6 * 0.1}[kind]
+        Ls = []
+        for sgn in (1, -1):
+            _restore(m64, warm64)
+            m64.time, m64.dt, m64.cfl_mult = ts64
+            vv, uu, aa = warm64["vxyz"].clone(), warm64["uint"].clone(), 0.1
+            if kind == "v":
+                vv[idx] += sgn * eps
+            elif kind == "u":
+                uu[idx] += sgn * eps
+            else:
+                aa += sgn * eps
+            with torch.no_grad():
+                x, v, u = adjoint.rollout(m64, vv, uu, torch.tensor(aa, dtype=torch.float64),
+                                          steps, ck, dts=dts)
+                Ls.append(float(((v - v_t) ** 2).sum()))
+        fd = (Ls[0] - Ls[1]) / (2 * eps)
+        a64 = g64[kind] if kind == "a" else float(g64[kind][idx])
+        a32 = g32[kind] if kind == "a" else float(g32[kind][idx])
+        res.append((kind, idx, a64, a32, fd))
+    big = {k: max(abs(r[4]) for r in res if r[0] == k) for k in ("v", "u", "a")}
+    errs = []
+    for kind, idx, a64, a32, fd in res:
+        den = max(abs(fd), 1e-3 * big[kind])
+        e64, e32 = abs(a64 - fd) / den, abs(a32 - fd) / den
+        print(f"{kind} {idx}: fd {fd:.8e} fp64 {a64:.8e} ({e64:.1e}) mixed {a32:.8e} ({e32:.1e})")
+        errs.append((e64, e32, kind, idx))
+    assert max(e[0] for e in errs if e[2] != "u") < 1e-4, errs
+    assert max(e[0] for e in errs if e[2] == "u") < 1e-2, errs
+    assert max(e[1] for e in errs) < 1e-2, errs
