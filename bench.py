@@ -42,6 +42,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--workload", default="sedov",
+                   choices=["sedov", "sedov_plain", "clustered", "soundwave"],
+                   help="sedov: jittered Sedov-Taylor (default, 4*cells^3); sedov_plain: the "
+                        "same without jitter; clustered: 8,388,608 particles, half uniform, "
+                        "half in a Gaussian clump; soundwave: 64^3 travelling sound wave")
     p.add_argument("--cells", type=int, default=64, help="FCC cells per axis (4*cells^3 particles)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -52,13 +57,27 @@ def parse():
     return p.parse_args()
 
 
-def workload(cells):
+def workload(cells, kind="sedov"):
+    """Seeded synthetic inputs with the shapes of the benchmark configurations (no
+    dataset is involved).  Returns (set-up dict, name, alpha_AV)."""
     from shamrock_gb300 import setups
 
-    s = setups.sedov_taylor(cells, jitter=0.05, seed=1)
-    name = (f"sedov_taylor_fcc_4x{cells}^3_jitter0.05_periodic (N={len(s['h'])}, M4, "
+    if kind == "clustered":
+        s = setups.clustered_box(8388608, seed=12345, sigma=0.05)
+        name = ("clustered_box_8388608 (half uniform, half Gaussian clump sigma 0.05, "
+                "v ~ N(0, 0.1^2), u ~ U[0.5, 1.5], gamma 5/3, M4, constant AV a=1 b=2, "
+                "CFL 0.3, periodic, tree rebuilt every step)")
+        return s, name, 1.0
+    if kind == "soundwave":
+        s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
+        name = ("sound_wave_cubic_64^3 (N=262144, amp 1e-4, gamma 1.0001, constant AV "
+                "a=0.1 b=2, CFL 0.3, periodic)")
+        return s, name, 0.1
+    jitter = 0.05 if kind == "sedov" else 0.0
+    s = setups.sedov_taylor(cells, jitter=jitter, seed=1)
+    name = (f"sedov_taylor_fcc_4x{cells}^3_jitter{jitter:g}_periodic (N={len(s['h'])}, M4, "
             "constant AV a=1 b=2, gamma=5/3, CFL 0.3, tree rebuilt every step)")
-    return s, name
+    return s, name, 1.0
 
 
 def make_model(s, precision, device=0, alpha_AV=1.0):
@@ -141,10 +160,11 @@ class ClockSampler:
 # L1/L2 hits; index streams and per-particle fields are counted).  units: rows (local
 # particles), entries (CSR entries), keys (sorted slots).
 def stage_bytes(stage, n, N, entries, P, precision, h_iters):
-    vec = 80 if precision == "mixed" else 88
+    vec = 64 if precision == "mixed" else 88
     table = {
-        # row_rank, row_local, cnt, off, own fields, CSR entries, caller a/du/v/u in+out, h
-        "derivs": n * (16 + vec + 128 + 8) + 4 * entries,
+        # row_rank, row_local, cnt, off, own fields, CSR entries, caller a/du/v/u in+out,
+        # h; every particle's record read once from DRAM (further gathers: L1/L2 hits)
+        "derivs": n * (16 + vec + 128 + 8) + 4 * entries + N * vec,
         # per Newton iteration: CSR entries + own position + per-row h/eps state
         "h_iterate": (n * (16 + (32 if precision == "mixed" else 24) + 40) + 4 * entries) * h_iters,
         "cache_fill": n * (4 + 4 + 4 + 32) + 4 * entries,
@@ -180,48 +200,75 @@ def roofline(prof, log, n, precision, peaks_path):
         out.update(achieved=achieved, frac=achieved / peak, algorithmic_bytes=nbytes)
     else:
         out.update(achieved=None, frac=None, algorithmic_bytes=None)
-    out["traffic"] = traffic_from_profiles(dom, N)
+    out["traffic"] = traffic_from_profiles(dom, n)
     out["stages_ms"] = {k: round(v, 4) for k, v in ms.items()}
     return out
 
 
-def traffic_from_profiles(stage, N):
-    """DRAM bytes per launch of `stage` from the committed ncu summary, scaled to N."""
+def traffic_from_profiles(stage, n):
+    """DRAM bytes per launch of `stage` from the committed ncu summary (bytes per local
+    particle of one launch), scaled to n local particles."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     try:
         for line in open(path):
             parts = line.split()
-            if len(parts) >= 3 and parts[0] == stage and not line.startswith("#"):
-                per_particle = float(parts[1])
-                return per_particle * N
-    except OSError:
+            if len(parts) >= 2 and parts[0] == stage and not line.startswith("#"):
+                return float(parts[1]) * n
+    except (OSError, ValueError):
         pass
     return None
 
 
 # ----------------------------------------------------------------------------- arms
-def dist_setup():
+def dist_setup(backend=None):
+    """Rank / world from the torchrun environment; a process group when world > 1
+    (NCCL on GPUs, gloo otherwise).  Ranks are independent replicas: the group only
+    carries the barrier and the max-over-ranks time."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
     if world > 1:
+        import torch
         import torch.distributed as dist
 
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
         pg = dist
     return world, rank, local, pg
 
 
-def cpu_baseline(s, seconds, threads=None):
+def max_over_ranks(t_ms, dist, device="cpu"):
+    """The slowest rank's time (the whole job ends when it does)."""
+    if dist is None:
+        return float(t_ms)
+    import torch
+
+    t = torch.tensor([float(t_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(n_per_rank, world, steps, t_max_ms):
+    """Particle-steps per second of all replicas together."""
+    return n_per_rank * world * steps / (t_max_ms * 1e-3)
+
+
+def reference_rank_runs(world, rank):
+    """Under torchrun the reference arm runs on rank 0 alone; other ranks exit 0."""
+    return world <= 1 or rank == 0
+
+
+def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     """FP64 oracle (OpenMP) on the same workload, bounded to about `seconds`."""
     from oracle import oracle as O
 
     if threads:
         O.set_threads(threads)
     cores = O.get_threads()
-    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0,
+    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0,
                      cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
                      htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
                      h_max_subcycles=100, tree_reduction_level=3, periodic=1)
@@ -246,14 +293,14 @@ def cpu_baseline(s, seconds, threads=None):
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    if world > 1 and rank != 0:
+    if not reference_rank_runs(world, rank):
         return 0
-    s, name = workload(args.cells)
+    s, name, alpha_av = workload(args.cells, args.workload)
     from oracle import oracle as O
 
     O.set_threads(os.cpu_count())
     cores = O.get_threads()
-    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=1.0, beta_AV=2.0,
+    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_av, beta_AV=2.0,
                      cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
                      htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
                      h_max_subcycles=100, tree_reduction_level=3, periodic=1)
@@ -290,7 +337,7 @@ def run_reference(args):
     return 0
 
 
-def accuracy(s, m_mixed_state=None):
+def accuracy(s, alpha_AV=1.0):
     """Max / RMS relative error of rho, |a|, du/dt and v_sig-driven dt of one mixed step
     against one FP64 step from the same initial state (the first, dt = 0, step)."""
     import numpy as np
@@ -298,7 +345,7 @@ def accuracy(s, m_mixed_state=None):
     res = {}
     d = {}
     for prec in ("fp64", "mixed"):
-        m = make_model(s, prec)
+        m = make_model(s, prec, alpha_AV=alpha_AV)
         m.evolve_once()
         d[prec] = m.collect_data()
     a, b = d["mixed"], d["fp64"]
@@ -326,9 +373,9 @@ def run_gb300(args):
 
     world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
-    s, name = workload(args.cells)
+    s, name, alpha_av = workload(args.cells, args.workload)
     n = len(s["h"])
-    m = make_model(s, args.precision, device=local)
+    m = make_model(s, args.precision, device=local, alpha_AV=alpha_av)
     lib = m._lib()
     for _ in range(max(args.warmup, 3)):
         m.evolve_once()
@@ -353,13 +400,8 @@ def run_gb300(args):
     prof = lib.profile_read()
     lib.profile(False)
     t_ms = e0.elapsed_time(e1)
-    t_max = t_ms
-    total_particles = n * world
-    if dist:
-        t = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = total_particles * args.steps / (t_max * 1e-3)
+    t_max = max_over_ranks(t_ms, dist, device="cuda")
+    value = whole_job_rate(n, world, args.steps, t_max)
     clk = clocks.summary()
 
     # end-to-end through the public API with host buffers, every step:
@@ -384,12 +426,8 @@ def run_gb300(args):
                 host[k].copy_(d[k], non_blocking=True)
         f1.record(stream)
         torch.cuda.synchronize()
-        te = f0.elapsed_time(f1)
-        if dist:
-            t = torch.tensor([te], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
-        e2e = {"value": total_particles * steps_e2e / (te * 1e-3), "unit": UNIT,
+        te = max_over_ranks(f0.elapsed_time(f1), dist, device="cuda")
+        e2e = {"value": whole_job_rate(n, world, steps_e2e, te), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "steps": steps_e2e}
 
     if rank != 0:
@@ -415,9 +453,9 @@ def run_gb300(args):
                                           "next_dt", "cfl_mult")},
     }
     if world == 1 and not args.no_accuracy:
-        line["accuracy_mixed_vs_fp64"] = accuracy(s)
+        line["accuracy_mixed_vs_fp64"] = accuracy(s, alpha_AV=alpha_av)
         # FP64 GPU rate on the same workload (the x3 denominator), a few steps
-        m64 = make_model(s, "fp64")
+        m64 = make_model(s, "fp64", alpha_AV=alpha_av)
         for _ in range(2):
             m64.evolve_once()
         torch.cuda.synchronize()
@@ -435,7 +473,8 @@ def run_gb300(args):
     if world == 1 and not args.no_adjoint:
         line["adjoint"] = adjoint_bench(precision=args.precision, device=local)
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(s, args.cpu_seconds, threads=os.cpu_count())
+        line["cpu_baseline"] = cpu_baseline(s, args.cpu_seconds, threads=os.cpu_count(),
+                                            alpha_AV=alpha_av)
     print(json.dumps(line), flush=True)
     return 0
 

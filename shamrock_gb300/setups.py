@@ -8,7 +8,8 @@ dataset is involved): every generator is deterministic given its seed.
   energy of the particles within r < r_inj * a of the centre (a = 1/n), optional
   Gaussian position jitter sigma * a.
 - ``clustered_box``: half the particles uniform in the unit cube, half in a
-  Gaussian clump (clipped into the box), v ~ N(0, 0.1^2), u ~ U[0.5, 1.5].
+  Gaussian clump, both sampled from jittered lattices (the clump by radial stretch
+  mapping), v ~ N(0, 0.1^2), u ~ U[0.5, 1.5].
 - ``sound_wave``: simple cubic lattice of 64^3 = 2^18 particles filling the periodic
   unit cube, with a 1e-4 sin(2 pi x) density perturbation applied by a position
   remap and the matching travelling-wave velocity (an FCC lattice cannot hold exactly 2^18 sites in a cube: 4*40^3 < 2^18, and
@@ -58,12 +59,54 @@ def sedov_taylor(n_cells, jitter=0.0, seed=1, E=1.0, u0=1e-5, r_inj=2.0, gamma=5
                 n_inject=n_inj)
 
 
-def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0):
+def _chi3_radius_table(n=4096, rmax=8.0):
+    """Radius of a 3-D standard normal vector against its cumulative probability
+    P(r) = erf(r / sqrt 2) - sqrt(2 / pi) r exp(-r^2 / 2), tabulated for inversion."""
+    from math import erf
+
+    r = np.linspace(0.0, rmax, n)
+    P = np.array([erf(x / np.sqrt(2.0)) for x in r]) - np.sqrt(2.0 / np.pi) * r * np.exp(-0.5 * r * r)
+    return P, r
+
+
+def _jittered_lattice(n_side, rng, jitter):
+    g = (np.arange(n_side) + 0.5) / n_side
+    i, j, k = np.meshgrid(g, g, g, indexing="ij")
+    pos = np.stack([i.ravel(), j.ravel(), k.ravel()], 1)
+    return pos + (jitter / n_side) * rng.standard_normal(pos.shape)
+
+
+def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0, jitter=0.1):
+    """Half the particles uniform in the unit cube, half in a Gaussian clump of width sigma
+    at the centre; v ~ N(0, 0.1^2) per component, u ~ U[0.5, 1.5].
+
+    Both halves are sampled from jittered cubic lattices (jitter 0.1 of the spacing),
+    not as independent random points: the uniform half is a lattice over the cube with
+    sites removed at random down to N/2; the clump is a lattice ball mapped radially so
+    that its mass profile is the Gaussian's (stretch mapping).  Independent random
+    points put some pairs far closer than the mean spacing; for such a particle the
+    density sum is dominated by close pairs, Omega < 0, and the h-rho Newton step of
+    IterateSmoothingLengthDensity moves h away from the root every iteration (h then
+    grows by the sub-cycle limit until it spans the box).  Lattice sampling keeps the
+    same density field without near-coincident pairs."""
     rng = np.random.default_rng(seed)
     n1 = N // 2
     n2 = N - n1
-    p1 = rng.random((n1, 3))
-    p2 = np.clip(rng.normal(0.5, sigma, size=(n2, 3)), 1e-9, 1.0 - 1e-9)
+    # uniform half: smallest cubic lattice with >= n1 sites, random sites removed
+    ns = int(np.ceil(n1 ** (1.0 / 3.0)))
+    p1 = _jittered_lattice(ns, rng, jitter)
+    p1 = np.mod(p1[rng.permutation(len(p1))[:n1]], 1.0)
+    # clump: lattice ball of radius 1 with n2 sites (closest to the centre), stretched
+    nb = int(np.ceil((n2 * 6.0 / np.pi) ** (1.0 / 3.0))) + 2
+    q = _jittered_lattice(nb, rng, jitter) * 2.0 - 1.0
+    rq = np.linalg.norm(q, axis=1)
+    keep = np.argsort(rq, kind="stable")[:n2]
+    q, rq = q[keep], rq[keep]
+    u_frac = (rq / rq.max()) ** 3 * (1.0 - 1e-9)  # uniform ball: mass fraction r^3
+    P, rt = _chi3_radius_table()
+    r_new = sigma * np.interp(u_frac, P, rt)
+    dirs = q / np.maximum(rq, 1e-300)[:, None]
+    p2 = np.clip(0.5 + dirs * r_new[:, None], 1e-9, 1.0 - 1e-9)
     pos = np.concatenate([p1, p2])
     vel = rng.normal(0.0, 0.1, size=(N, 3))
     u = rng.uniform(0.5, 1.5, size=N)
