@@ -281,6 +281,13 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
 uint32_t gbsph_profile_kinds(void);
 /* Number of kernels this library has launched in the process so far. */
 uint64_t gbsph_kernel_launches(void);
+
+/* Memory budget of the neighbour cache's one-pass slots (bytes; 0 = the library
+ * default, 24 GiB).  Both cache stages are first built in one pass into fixed slots per
+ * leaf / per particle; a build that overflows is rerun with slots sized to its largest
+ * row, and when those would exceed the budget the exact two-pass build (count, scan,
+ * fill) runs instead.  The resulting cache is identical either way. */
+int gbsph_set_cache_budget(gbsph_ctx *ctx, uint64_t bytes);
 const char *gbsph_profile_name(uint32_t kind);
 int gbsph_profile_enable(gbsph_ctx *ctx, int on);
 int gbsph_profile_read(gbsph_ctx *ctx, double *ms_host, uint64_t *launches_host,

@@ -100,6 +100,7 @@ SIGNATURES = {
                                      _P(Cotangents), _P(_f64), _vp]),
     "gbsph_profile_kinds": (_u32, []),
     "gbsph_kernel_launches": (_u64, []),
+    "gbsph_set_cache_budget": (C.c_int, [_vp, _u64]),
     "gbsph_profile_name": (C.c_char_p, [_u32]),
     "gbsph_profile_enable": (C.c_int, [_vp, C.c_int]),
     "gbsph_profile_read": (C.c_int, [_vp, _vp, _vp, _vp, _u32]),

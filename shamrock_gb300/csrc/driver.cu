@@ -201,6 +201,14 @@ uint32_t gbsph_profile_kinds(void) { return kProfCount; }
 
 uint64_t gbsph_kernel_launches(void) { return g_kernel_launches; }
 
+int gbsph_set_cache_budget(gbsph_ctx *ctx, uint64_t bytes) {
+    if (!ctx) return GBSPH_ERR_ARG;
+    ctx->c.slot_budget = bytes;
+    ctx->c.leaf_cap    = 0;
+    ctx->c.row_cap     = 0;
+    return GBSPH_OK;
+}
+
 const char *gbsph_profile_name(uint32_t kind) {
     return kind < kProfCount ? kProfNames[kind] : "";
 }

@@ -37,6 +37,8 @@ struct Scalars {
     u32 ghost_total;
     u32 iters_max;     // max Newton iterations used by any particle
     u32 flags;         // error flags raised by kernels
+    u32 leaf_cnt_max;  // largest stage-1 list among leaves that overflowed their slots
+    u32 row_cnt_max;   // largest stage-2 row among rows that overflowed their slots
     u32 pad;
 };
 
@@ -112,6 +114,8 @@ struct Ctx {
 
     // ---- neighbour cache
     u64 leaf_csr_total = 0, csr_total = 0;
+    u32 leaf_cap = 0, row_cap = 0; // one-pass slots per leaf / row (grown on overflow)
+    u64 slot_budget = 0;            // bytes of one-pass slots allowed (0: library default)
     DevBuf leaf_cnt, leaf_off, leaf_ent; // stage 1 (leaf ids)
     DevBuf owner;                        // per row: leaf index
     DevBuf csr_cnt, csr_off, csr_ent;    // stage 2, per row, entries are ranks

@@ -13,6 +13,7 @@
 
 #include "gbsph_ctx.cuh"
 
+#include <cstddef>
 #include <type_traits>
 
 namespace gbsph {
@@ -20,8 +21,13 @@ namespace gbsph {
 namespace {
 
 constexpr int kStack   = 64;
-constexpr u32 kLeafCap = 256; // stage-1 slots per leaf in the one-pass build
-constexpr u32 kRowCap  = 192; // stage-2 slots per row in the one-pass build (multiple of 4)
+// Initial one-pass slots: stage-1 leaves per leaf, stage-2 entries per row (multiple of
+// 4).  A build that overflows records its largest row and is rerun, still in one pass,
+// with slots that fit; the context keeps the grown sizes for later builds.
+constexpr u32 kLeafCap = 256;
+constexpr u32 kRowCap  = 192;
+// Beyond this many slot bytes (or u32 offsets) the exact two-pass builds run instead.
+constexpr u64 kMaxSlotBytes = 24ull << 30;
 
 __device__ __forceinline__ void load_box(const NodeBox *__restrict__ b, f64 lo[3], f64 hi[3],
                                          f64 &rint) {
@@ -121,7 +127,7 @@ __global__ void k_leaf_fill(TreeView t, const u32 *__restrict__ off, u32 *__rest
     dfs(t, crit, [&](u32 leaf) { ent[w++] = leaf; });
 }
 
-// ---- stage 1, one pass into kLeafCap slots per leaf, optional FP32 pre-test.
+// ---- stage 1, one pass into `cap` slots per leaf, optional FP32 pre-test.
 // For boxes a (the leaf) and n (a node) the criterion is
 //   C1 || C2,  C1 = a overlaps n grown by r_n,  C2 = a grown by r_a overlaps n,
 // which in exact arithmetic is  max_axis s <= max(r_n, r_a)  with the per-axis
@@ -140,11 +146,11 @@ __global__ void k_boxes_f32(const NodeBox *__restrict__ b, u32 T, NodeBoxF *__re
 
 __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *__restrict__ fb,
                                                     u32 *__restrict__ cnt, u32 *__restrict__ off,
-                                                    u32 *__restrict__ ent, u32 *__restrict__ flags) {
+                                                    u32 *__restrict__ ent, u32 cap, Scalars *sc) {
     u32 l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= t.L) return;
     LeafCrit crit(t, l);
-    u32 c = 0, base = l * kLeafCap;
+    u32 c = 0, base = l * cap;
     bool ok;
     if (fb) {
         F8 fa = ldg256(&fb[t.off() + l]), fr = ldg256(&fb[0]);
@@ -168,17 +174,20 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
                 return crit(node);
             },
             [&](u32 leaf) {
-                if (c < kLeafCap) ent[base + c] = leaf;
+                if (c < cap) ent[base + c] = leaf;
                 c++;
             });
     } else {
         ok = dfs(t, crit, [&](u32 leaf) {
-            if (c < kLeafCap) ent[base + c] = leaf;
+            if (c < cap) ent[base + c] = leaf;
             c++;
         });
     }
-    if (!ok) atomicOr(flags, kFlagStackOverflow);
-    if (c > kLeafCap) atomicOr(flags, kFlagLeafCap);
+    if (!ok) atomicOr(&sc->flags, kFlagStackOverflow);
+    if (c > cap) {
+        atomicOr(&sc->flags, kFlagLeafCap);
+        atomicMax(&sc->leaf_cnt_max, c);
+    }
     cnt[l] = c;
     off[l] = base;
 }
@@ -242,7 +251,7 @@ __global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows
 // ---- stage 2 (NeighbourCache.cpp:492-591)
 // MODE kCount: per-row count, and the count rounded up to 4 into off[] (scanned in
 // place into offsets); kFill: entries at off[row]; kOnePass: entries straight into
-// kRowCap slots per row (off[row] = row * kRowCap), flagging kFlagCsrCap when a row
+// `cap` slots per row (off[row] = row * cap), flagging kFlagCsrCap when a row
 // overflows so the host reruns the two-pass build.  Either way every row starts on a
 // 16-byte boundary, so readers may fetch entries four at a time.
 //
@@ -260,7 +269,7 @@ __global__ void __launch_bounds__(256) k_part_cache(
     const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const float4 *__restrict__ P,
     const f64 *__restrict__ sx, const f64 *__restrict__ sy, const f64 *__restrict__ sz,
     const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ cnt, u32 *__restrict__ off,
-    u32 *__restrict__ ent, Scalars *sc) {
+    u32 *__restrict__ ent, Scalars *sc, u32 cap) {
     u32 row = blockIdx.x * blockDim.x + threadIdx.x;
     u32 c   = 0;
     if (row < n_rows) {
@@ -277,7 +286,7 @@ __global__ void __launch_bounds__(256) k_part_cache(
         const float lo_f = 1.f - 1e-5f, hi_f = 1.f + 1e-5f;
         u32 leaf = owner[row];
         u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
-        u32 w = (MODE == kFill) ? off[row] : ((MODE == kOnePass) ? row * kRowCap : 0);
+        u32 w = (MODE == kFill) ? off[row] : ((MODE == kOnePass) ? row * cap : 0);
         for (u32 k = k0; k < k1; k++) {
             u32 lb = leaf_ent[k];
             u32 r0 = reduc[lb], r1 = reduc[lb + 1];
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(256) k_part_cache(
                 }
                 if (in) {
                     if (MODE == kFill) ent[w + c] = rb;
-                    if (MODE == kOnePass && c < kRowCap) ent[w + c] = rb;
+                    if (MODE == kOnePass && c < cap) ent[w + c] = rb;
                     c++;
                 }
             }
@@ -315,7 +324,10 @@ __global__ void __launch_bounds__(256) k_part_cache(
         if (MODE == kCount) off[row] = (c + 3u) & ~3u;
         if (MODE == kOnePass) {
             off[row] = w;
-            if (c > kRowCap) atomicOr(&sc->flags, kFlagCsrCap);
+            if (c > cap) {
+                atomicOr(&sc->flags, kFlagCsrCap);
+                atomicMax(&sc->row_cnt_max, c);
+            }
         }
     }
     if (MODE != kCount) {
@@ -401,10 +413,18 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     Scalars *dsc = c.d_scalars.as<Scalars>();
     if ((e = c.leaf_cnt.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
     if ((e = c.leaf_off.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
-    // Stage 1 in one pass into kLeafCap slots per leaf; a leaf with more candidates
-    // raises kFlagLeafCap and the two-pass exact build below runs instead.
-    if ((e = cudaMemsetAsync(&dsc->flags, 0, sizeof(u32), s)) != cudaSuccess) return e;
-    if ((e = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * kLeafCap + 1), s)) != cudaSuccess) return e;
+    // Stage 1 in one pass into c.leaf_cap slots per leaf; if a leaf has more candidates
+    // the pass is rerun with slots that fit, or, past the slot budget, the exact
+    // two-pass build runs.
+    // flags, leaf_cnt_max and row_cnt_max are adjacent u32 fields of Scalars
+    static_assert(offsetof(Scalars, leaf_cnt_max) == offsetof(Scalars, flags) + 4 &&
+                      offsetof(Scalars, row_cnt_max) == offsetof(Scalars, flags) + 8,
+                  "Scalars field order");
+    if ((e = cudaMemsetAsync(&dsc->flags, 0, 3 * sizeof(u32), s)) != cudaSuccess) return e;
+    if (c.leaf_cap == 0) c.leaf_cap = kLeafCap;
+    const u64 budget = c.slot_budget ? c.slot_budget : kMaxSlotBytes;
+    auto slots_ok = [&](u64 rows, u32 cap) { return rows * cap < 0xffffffffull && rows * cap * 4 <= budget; };
+    const bool s1_one_pass = slots_ok(L, c.leaf_cap);
     const NodeBoxF *fb = nullptr;
     if (P) {
         u32 T = 2 * L - 1;
@@ -412,9 +432,21 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         { k_boxes_f32<<<div_up(T, 256), 256, 0, s>>>(c.boxes.as<NodeBox>(), T, c.fboxes.as<NodeBoxF>()); GBSPH_COUNTED; }
         fb = c.fboxes.as<NodeBoxF>();
     }
-    {
+    auto stage1 = [&]() -> cudaError_t {
+        cudaError_t err = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * c.leaf_cap + 1), s);
+        if (err != cudaSuccess) return err;
         ProfScope ps(c, kProfStage1, L);
-        { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
+        { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
+                                                    c.leaf_ent.as<u32>(), c.leaf_cap, dsc); GBSPH_COUNTED; }
+        return cudaGetLastError();
+    };
+    if (s1_one_pass) {
+        if ((e = stage1()) != cudaSuccess) return e;
+    } else {
+        // slots beyond the budget: flag the overflow so the exact build below runs
+        const u32 ovf = kFlagLeafCap;
+        if ((e = cudaMemcpyAsync(&dsc->flags, &ovf, sizeof(u32), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(&dsc->leaf_cnt_max, &c.leaf_cap, sizeof(u32), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
     }
     if ((e = c.owner.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
     if (n) {
@@ -430,24 +462,35 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     }
     c.leaf_csr_total = 0;
     if (c.h_scalars->flags & kFlagLeafCap) {
-        // some leaf has more than kLeafCap candidate leaves: exact two-pass build
-        ProfScope ps(c, kProfStage1, 0);
-        { k_leaf_count<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_cnt.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
-        if ((e = scan_exclusive_u32(c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), L, &dsc->total,
-                                    c.scan_scratch, s)) != cudaSuccess)
-            return e;
-        if ((e = sync_scalars(c)) != cudaSuccess) return e;
-        c.leaf_csr_total = c.h_scalars->total;
-        if ((e = c.leaf_ent.ensure(sizeof(u32) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
-        { k_leaf_fill<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_off.as<u32>(), c.leaf_ent.as<u32>()); GBSPH_COUNTED; }
+        const u32 cap = (c.h_scalars->leaf_cnt_max + 31u) & ~31u;
+        const bool fits = s1_one_pass && slots_ok(L, cap);
+        if ((e = cudaMemsetAsync(&dsc->flags, 0, sizeof(u32), s)) != cudaSuccess) return e;
+        if (fits) {
+            // one pass again with slots that hold the largest list
+            c.leaf_cap = cap;
+            if ((e = stage1()) != cudaSuccess) return e;
+        } else {
+            // exact two-pass build
+            ProfScope ps(c, kProfStage1, 0);
+            { k_leaf_count<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_cnt.as<u32>(), &dsc->flags); GBSPH_COUNTED; }
+            if ((e = scan_exclusive_u32(c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(), L, &dsc->total,
+                                        c.scan_scratch, s)) != cudaSuccess)
+                return e;
+            if ((e = sync_scalars(c)) != cudaSuccess) return e;
+            c.leaf_csr_total = c.h_scalars->total;
+            if ((e = c.leaf_ent.ensure(sizeof(u32) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
+            { k_leaf_fill<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_off.as<u32>(), c.leaf_ent.as<u32>()); GBSPH_COUNTED; }
+        }
     }
 
     if ((e = c.csr_cnt.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
     if ((e = c.csr_off.ensure(sizeof(u32) * ((size_t) n + 1), s)) != cudaSuccess) return e;
-    // the padded one-pass layout needs row * kRowCap to fit the u32 offsets
-    const bool one_pass = (u64) n * kRowCap < 0xffffffffull;
+    // the padded one-pass layout needs row * cap to fit the u32 offsets
+    if (c.row_cap == 0) c.row_cap = kRowCap;
+    auto slots_fit = [&](u32 cap) { return slots_ok(n, cap); };
+    bool one_pass = slots_fit(c.row_cap);
     if (one_pass)
-        if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * kRowCap + 4), s)) != cudaSuccess) return e;
+        if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * c.row_cap + 4), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(&dsc->csr_entries, 0, sizeof(u64), s)) != cudaSuccess) return e;
     // launch helper for the stage-2 kernel family
     auto part = [&](auto mode_tag, u32 *cnt, u32 *off, u32 *ent) {
@@ -456,13 +499,13 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
             { k_part_cache<MODE, true><<<div_up(n, 256), 256, 0, s>>>(
                 c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
                 c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), P, c.sx.as<f64>(),
-                c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off, ent, dsc); GBSPH_COUNTED; }
+                c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off, ent, dsc, c.row_cap); GBSPH_COUNTED; }
         } else {
             { k_part_cache<MODE, false><<<div_up(n, 256), 256, 0, s>>>(
                 c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
                 c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), nullptr,
                 c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off,
-                ent, dsc); GBSPH_COUNTED; }
+                ent, dsc, c.row_cap); GBSPH_COUNTED; }
         }
     };
     using OnePass = std::integral_constant<int, kOnePass>;
@@ -474,8 +517,26 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     }
     if ((e = sync_scalars(c)) != cudaSuccess) return e;
     c.csr_total = c.h_scalars->csr_entries;
+    if (n && one_pass && (c.h_scalars->flags & kFlagCsrCap)) {
+        // a row overflowed: one pass again with slots that hold the largest row
+        const u32 cap = (c.h_scalars->row_cnt_max + 3u) & ~3u;
+        if (slots_fit(cap)) {
+            c.row_cap = cap;
+            if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * cap + 4), s)) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(&dsc->csr_entries, 0, sizeof(u64), s)) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(&dsc->flags, 0, sizeof(u32), s)) != cudaSuccess) return e;
+            {
+                ProfScope ps(c, kProfCacheFill, n);
+                part(OnePass{}, c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>());
+            }
+            if ((e = sync_scalars(c)) != cudaSuccess) return e;
+            c.csr_total = c.h_scalars->csr_entries;
+        } else {
+            one_pass = false;
+        }
+    }
     if (n && (!one_pass || (c.h_scalars->flags & kFlagCsrCap))) {
-        // a row has more than kRowCap entries: two-pass build into a compact CSR
+        // slots beyond the budget: exact two-pass build into a compact CSR
         {
             ProfScope ps(c, kProfCacheCount, n);
             part(Count{}, c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), nullptr);

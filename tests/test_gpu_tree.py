@@ -173,6 +173,34 @@ def test_neighbour_cache_vs_oracle(gctx, M, n_cells, jitter, level, precision):
     assert np.array_equal(csr["entries"].cpu().numpy().view(np.uint32), oc["entries"])
 
 
+@pytest.mark.parametrize("budget", [1 << 10, None])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_neighbour_cache_slot_paths(gctx, M, budget, precision):
+    """h three times the lattice estimate puts ~27x the usual neighbours in every row,
+    overflowing the initial one-pass slots (256 leaves, 192 entries): with the default
+    budget the builds rerun in one pass with grown slots, with a 1 KiB budget the exact
+    two-pass builds run.  Both give the oracle's cache bit for bit."""
+    s = _lattice(10, 0.05, 9)
+    n = len(s["h"])
+    h = s["h"] * 3.0
+    g = M.periodic_ghosts(gctx, s["pos"], h, [0, 0, 0], [1, 1, 1], 1.1)
+    mpos, mh = g["merged_pos"], g["merged_h"]
+    lo = np.nextafter(mpos.min(0), -np.inf)
+    hi = np.nextafter(mpos.max(0), np.inf)
+    gctx.call("gbsph_set_cache_budget", 0 if budget is None else budget)
+    try:
+        t = M.Tree(gctx, mpos, lo, hi, 3, h=mh, htol=1.1)
+        csr = M.neighbour_cache(gctx, n, 1.1, precision)
+    finally:
+        gctx.call("gbsph_set_cache_budget", 0)
+    o = O.Tree(mpos, lo, hi, 3, h=mh, htol=1.1)
+    oc = o.neigh_cache(mpos, mh, n, 1.1)
+    assert oc["cnt"].max() > 192
+    assert np.array_equal(csr["cnt"].cpu().numpy().view(np.uint32), oc["cnt"])
+    assert np.array_equal(csr["scanned"].cpu().numpy().view(np.uint32), oc["scanned"])
+    assert np.array_equal(csr["entries"].cpu().numpy().view(np.uint32), oc["entries"])
+
+
 def test_sort_properties_large(gctx, M):
     """Size-independent properties at 2^24 keys: sorted output, permutation, stable pairing."""
     n = 1 << 24
