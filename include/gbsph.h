@@ -240,6 +240,26 @@ int gbsph_periodic_ghosts(gbsph_ctx *ctx, gbsph_vec3 xyz, const double *h, uint3
 int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double *mx, double *my,
                        double *mz, double *mh, void *stream);
 
+/* Leapfrog predictor of Solver::evolve_once (Solver.cpp:390-524 with
+ * shamrock/src/math/integrators.cpp:27-86): v += dt/2 a, u += dt/2 du, x += dt v, then
+ * the second half kick; with periodic != 0 the positions are wrapped into the box
+ * (integrators.cpp:207-237).  In place on p's xyz, vxyz, uint (reads axyz, duint). */
+int gbsph_kdk_predict(gbsph_ctx *ctx, const gbsph_particles *p, double dt, uint32_t periodic,
+                      const double bmin_host[3], const double bmax_host[3], void *stream);
+
+/* Leapfrog corrector (integrators.cpp:88-120, Solver.cpp:2506-2616): with p's axyz / duint
+ * holding the new derivatives, v += dt/2 (a_new - a_old), u += dt/2 (du_new - du_old);
+ * *eps_v_host = max |dv| / sqrt(sum v^2 / n), the corrector's rerun test (0 when the
+ * mean vanishes). */
+int gbsph_kdk_correct(gbsph_ctx *ctx, const gbsph_particles *p, gbsph_vec3 a_old,
+                      const double *du_old, double dt, double *eps_v_host, void *stream);
+
+/* CFL time step (ComputeCFLCourant.hpp:45-60, ComputeCFLForce.hpp:50-62) per particle,
+ * dt_a = min(C_cour h / v_sig, C_force sqrt(h / |a|)), into dt_part (optional), and its
+ * minimum over the particles (Solver.cpp:3046-3119) into *dt_min_host. */
+int gbsph_cfl(gbsph_ctx *ctx, const double *h, const double *vsig, gbsph_vec3 a, uint32_t n,
+              double C_cour, double C_force, double *dt_part, double *dt_min_host, void *stream);
+
 /* ------------------------------------------------------------------ full step */
 
 /* One Solver::evolve_once on one patch (shammodels/sph/src/Solver.cpp:1942-3272):

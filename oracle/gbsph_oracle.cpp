@@ -805,6 +805,64 @@ f64 cfl_min(u32 n, const f64 *h, const f64 *vsig, const f64 *axyz, f64 C_cour, f
     return m;
 }
 
+// Leapfrog predictor — shamrock/src/math/integrators.cpp:27-86 via Solver.cpp:390-524:
+// v += dt/2 a, u += dt/2 du (half step 1), x += dt v, then the second half step, and the
+// periodic wrap of the positions (integrators.cpp:207-237).
+void leapfrog_predict(u32 n, f64 *xyz, f64 *vxyz, f64 *u, const f64 *axyz, const f64 *du, f64 dt,
+                      u32 periodic, const f64 *bmin, const f64 *bmax) {
+    const f64 dt_half = dt / 2;
+    for (u32 i = 0; i < n; i++) {
+        for (int c = 0; c < 3; c++) vxyz[3 * i + c] = vxyz[3 * i + c] + dt_half * axyz[3 * i + c];
+        u[i] = u[i] + dt_half * du[i];
+    }
+    for (u32 i = 0; i < 3 * n; i++) xyz[i] = xyz[i] + dt * vxyz[i];
+    for (u32 i = 0; i < n; i++) {
+        for (int c = 0; c < 3; c++) vxyz[3 * i + c] = vxyz[3 * i + c] + dt_half * axyz[3 * i + c];
+        u[i] = u[i] + dt_half * du[i];
+    }
+    if (periodic) {
+        for (u32 i = 0; i < n; i++)
+            for (int c = 0; c < 3; c++) {
+                f64 delt = bmax[c] - bmin[c];
+                f64 r    = xyz[3 * i + c] - bmin[c];
+                r        = std::fmod(r, delt);
+                r += delt;
+                r = std::fmod(r, delt);
+                r += bmin[c];
+                xyz[3 * i + c] = r;
+            }
+    }
+}
+
+// Leapfrog corrector — integrators.cpp:88-120, Solver.cpp:2506-2616: v += dt/2 (a_new -
+// a_old), u += dt/2 (du_new - du_old); returns eps_v = max|dv| / sqrt(sum v^2 / n) (0
+// when the mean vanishes), the rerun test of the corrector loop.
+f64 leapfrog_correct(u32 n, f64 *vxyz, f64 *u, const f64 *a_new, const f64 *a_old,
+                     const f64 *du_new, const f64 *du_old, f64 dt) {
+    f64 hdt     = dt / 2;
+    f64 max_ev2 = 0;
+    for (u32 i = 0; i < n; i++) {
+        f64 ix = hdt * (a_new[3 * i] - a_old[3 * i]);
+        f64 iy = hdt * (a_new[3 * i + 1] - a_old[3 * i + 1]);
+        f64 iz = hdt * (a_new[3 * i + 2] - a_old[3 * i + 2]);
+        vxyz[3 * i]     = vxyz[3 * i] + ix;
+        vxyz[3 * i + 1] = vxyz[3 * i + 1] + iy;
+        vxyz[3 * i + 2] = vxyz[3 * i + 2] + iz;
+        max_ev2         = std::fmax(max_ev2, ix * ix + iy * iy + iz * iz);
+        f64 iu          = hdt * (du_new[i] - du_old[i]);
+        u[i]            = u[i] + iu;
+    }
+    f64 sum_vsq = 0;
+    for (u32 i = 0; i < n; i++)
+        sum_vsq += vxyz[3 * i] * vxyz[3 * i] + vxyz[3 * i + 1] * vxyz[3 * i + 1]
+                   + vxyz[3 * i + 2] * vxyz[3 * i + 2];
+    f64 rank_veps_v = std::sqrt(max_ev2);
+    f64 vmean       = std::sqrt(sum_vsq / f64(n));
+    f64 eps_v       = rank_veps_v / vmean;
+    if (vmean <= 0) eps_v = 0;
+    return eps_v;
+}
+
 // =================================================================================
 // Periodic ghosts, one patch covering the box —
 //   find_interfaces shammodels/sph/src/BasicSPHGhosts.cpp:260-360 (27 offsets, x
@@ -914,34 +972,13 @@ void evolve_once(Sim &s, StepLog &log) {
     const Config &cfg = s.cfg;
     u32 n             = s.n;
     f64 dt            = s.dt;
-    f64 dt_half       = dt / 2;
     log               = StepLog{};
     log.t             = s.t;
     log.dt            = dt;
     log.n_local       = n;
 
-    // leapfrog predictor: half_step1 (v then u), full_step_xyz, half_step2
-    for (u32 i = 0; i < n; i++) {
-        for (int c = 0; c < 3; c++) s.vxyz[3 * i + c] = s.vxyz[3 * i + c] + dt_half * s.axyz[3 * i + c];
-        s.u[i] = s.u[i] + dt_half * s.du[i];
-    }
-    for (u32 i = 0; i < 3 * n; i++) s.xyz[i] = s.xyz[i] + dt * s.vxyz[i];
-    for (u32 i = 0; i < n; i++) {
-        for (int c = 0; c < 3; c++) s.vxyz[3 * i + c] = s.vxyz[3 * i + c] + dt_half * s.axyz[3 * i + c];
-        s.u[i] = s.u[i] + dt_half * s.du[i];
-    }
-    if (cfg.periodic) {
-        for (u32 i = 0; i < n; i++)
-            for (int c = 0; c < 3; c++) {
-                f64 delt = cfg.bmax[c] - cfg.bmin[c];
-                f64 r    = s.xyz[3 * i + c] - cfg.bmin[c];
-                r        = std::fmod(r, delt);
-                r += delt;
-                r = std::fmod(r, delt);
-                r += cfg.bmin[c];
-                s.xyz[3 * i + c] = r;
-            }
-    }
+    leapfrog_predict(n, s.xyz.data(), s.vxyz.data(), s.u.data(), s.axyz.data(), s.du.data(), dt,
+                     cfg.periodic, cfg.bmin, cfg.bmax);
 
     // sph_prestep
     std::vector<f64> mxyz, mh;
@@ -1020,27 +1057,8 @@ void evolve_once(Sim &s, StepLog &log) {
                        s.cache.part.entries.data(), mxyz.data(), m_v.data(), m_h.data(),
                        m_om.data(), m_u.data(), s.P.data(), s.cs.data(), cfg.pmass, cfg.alpha_u,
                        cfg.alpha_AV, cfg.beta_AV, s.axyz.data(), s.du.data());
-        f64 hdt     = dt / 2;
-        f64 max_ev2 = 0;
-        for (u32 i = 0; i < n; i++) {
-            f64 ix = hdt * (s.axyz[3 * i] - old_a[3 * i]);
-            f64 iy = hdt * (s.axyz[3 * i + 1] - old_a[3 * i + 1]);
-            f64 iz = hdt * (s.axyz[3 * i + 2] - old_a[3 * i + 2]);
-            s.vxyz[3 * i]     = s.vxyz[3 * i] + ix;
-            s.vxyz[3 * i + 1] = s.vxyz[3 * i + 1] + iy;
-            s.vxyz[3 * i + 2] = s.vxyz[3 * i + 2] + iz;
-            max_ev2           = std::fmax(max_ev2, ix * ix + iy * iy + iz * iz);
-            f64 iu            = hdt * (s.du[i] - old_du[i]);
-            s.u[i]            = s.u[i] + iu;
-        }
-        f64 sum_vsq = 0;
-        for (u32 i = 0; i < n; i++)
-            sum_vsq += s.vxyz[3 * i] * s.vxyz[3 * i] + s.vxyz[3 * i + 1] * s.vxyz[3 * i + 1]
-                       + s.vxyz[3 * i + 2] * s.vxyz[3 * i + 2];
-        f64 rank_veps_v = std::sqrt(max_ev2);
-        f64 vmean       = std::sqrt(sum_vsq / f64(n));
-        f64 eps_v       = rank_veps_v / vmean;
-        if (vmean <= 0) eps_v = 0;
+        f64 eps_v = leapfrog_correct(n, s.vxyz.data(), s.u.data(), s.axyz.data(), old_a.data(),
+                                     s.du.data(), old_du.data(), dt);
         log.eps_v = eps_v;
         if (eps_v > 1e-2) {
             rerun = true;
@@ -1231,6 +1249,14 @@ void orc_vsig(u32 n, const u32 *cnt, const u32 *sc, const u32 *ent, const f64 *x
 }
 f64 orc_cfl(u32 n, const f64 *h, const f64 *vsig, const f64 *a, f64 cc, f64 cf, f64 *dt_part) {
     return orc::cfl_min(n, h, vsig, a, cc, cf, dt_part);
+}
+void orc_predict(u32 n, f64 *xyz, f64 *vxyz, f64 *u, const f64 *axyz, const f64 *du, f64 dt,
+                 u32 periodic, const f64 *bmin, const f64 *bmax) {
+    orc::leapfrog_predict(n, xyz, vxyz, u, axyz, du, dt, periodic, bmin, bmax);
+}
+f64 orc_correct(u32 n, f64 *vxyz, f64 *u, const f64 *a_new, const f64 *a_old, const f64 *du_new,
+                const f64 *du_old, f64 dt) {
+    return orc::leapfrog_correct(n, vxyz, u, a_new, a_old, du_new, du_old, dt);
 }
 u32 orc_periodic_ghosts(u32 n, const f64 *xyz, const f64 *h, const f64 *bmin, const f64 *bmax,
                         f64 htol, u32 *src_out, f64 *off_out, u32 cap) {

@@ -100,6 +100,10 @@ def lib():
                                       C.c_double, _f64p, _f64p]),
         "orc_vsig": (None, [C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p, _f64p, _f64p]),
         "orc_cfl": (C.c_double, [C.c_uint32, _f64p, _f64p, _f64p, C.c_double, C.c_double, _vp]),
+        "orc_predict": (None, [C.c_uint32, _f64p, _f64p, _f64p, _f64p, _f64p, C.c_double,
+                               C.c_uint32, _f64p, _f64p]),
+        "orc_correct": (C.c_double, [C.c_uint32, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p,
+                                     C.c_double]),
         "orc_periodic_ghosts": (C.c_uint32, [C.c_uint32, _f64p, _f64p, _f64p, _f64p, C.c_double,
                                              _vp, _vp, C.c_uint32]),
         "orc_sim_create": (_vp, [C.POINTER(OrcConfig), C.c_uint32, _f64p, _f64p, _f64p, _f64p]),
@@ -292,6 +296,22 @@ def cfl(h, vsig_, a, C_cour, C_force):
     dtp = np.zeros(len(h))
     m = lib().orc_cfl(len(h), h, _f64(vsig_), _f64(a, (-1, 3)), C_cour, C_force, _ptr(dtp))
     return m, dtp
+
+
+def predict(pos, v, u, a, du, dt, periodic, bmin, bmax):
+    """Leapfrog predictor + periodic wrap; returns new (pos, v, u)."""
+    pos, v, u = _f64(pos, (-1, 3)).copy(), _f64(v, (-1, 3)).copy(), _f64(u).copy()
+    lib().orc_predict(len(u), pos, v, u, _f64(a, (-1, 3)), _f64(du), dt, int(periodic),
+                      _f64(bmin), _f64(bmax))
+    return pos, v, u
+
+
+def correct(v, u, a_new, a_old, du_new, du_old, dt):
+    """Leapfrog corrector; returns new (v, u) and eps_v."""
+    v, u = _f64(v, (-1, 3)).copy(), _f64(u).copy()
+    e = lib().orc_correct(len(u), v, u, _f64(a_new, (-1, 3)), _f64(a_old, (-1, 3)), _f64(du_new),
+                          _f64(du_old), dt)
+    return v, u, e
 
 
 def periodic_ghosts(pos, h, bmin, bmax, htol):

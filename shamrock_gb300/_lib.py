@@ -96,6 +96,9 @@ SIGNATURES = {
     "gbsph_ghost_export": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbsph_evolve_once": (C.c_int, [_vp, _P(Particles), _P(Config), _P(TimeState), _P(StepLog),
                                     _vp]),
+    "gbsph_kdk_predict": (C.c_int, [_vp, _P(Particles), _f64, _u32, _P(_f64), _P(_f64), _vp]),
+    "gbsph_kdk_correct": (C.c_int, [_vp, _P(Particles), Vec3, _vp, _f64, _P(_f64), _vp]),
+    "gbsph_cfl": (C.c_int, [_vp, _vp, _vp, Vec3, _u32, _f64, _f64, _vp, _P(_f64), _vp]),
     "gbsph_adjoint_step": (C.c_int, [_vp, _P(Particles), _P(Config), _f64, _f64, _u32,
                                      _P(Cotangents), _P(_f64), _vp]),
     "gbsph_profile_kinds": (_u32, []),

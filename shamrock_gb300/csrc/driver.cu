@@ -448,6 +448,58 @@ int gbsph_eos_adiabatic(gbsph_ctx *ctx, const double *h, const double *u, uint32
     return GBSPH_OK;
 }
 
+int gbsph_kdk_predict(gbsph_ctx *ctx, const gbsph_particles *p, double dt, uint32_t periodic,
+                      const double *bmin_host, const double *bmax_host, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(p && p->n > 0, "empty patch");
+    REQUIRE_ARG(!periodic || (bmin_host && bmax_host), "the periodic wrap needs the box");
+    REQUIRE_ARG(p->xyz.stride == p->vxyz.stride && p->xyz.stride == p->axyz.stride,
+                "xyz, vxyz and axyz must share one element stride");
+    LocalFields lf{p->xyz.x,  p->xyz.y,  p->xyz.z,  p->vxyz.x, p->vxyz.y,  p->vxyz.z,
+                   p->axyz.x, p->axyz.y, p->axyz.z, p->xyz.stride, p->hpart, p->uint, p->duint};
+    const f64 zero[3] = {0, 0, 0};
+    CU(predict64(c, lf, p->n, dt, periodic ? 1 : 0, periodic ? bmin_host : zero,
+                 periodic ? bmax_host : zero));
+    CU(cudaStreamSynchronize(c.stream));
+    return GBSPH_OK;
+}
+
+int gbsph_kdk_correct(gbsph_ctx *ctx, const gbsph_particles *p, gbsph_vec3 a_old,
+                      const double *du_old, double dt, double *eps_v_host, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(p && p->n > 0, "empty patch");
+    REQUIRE_ARG(a_old.x && a_old.y && a_old.z && du_old, "a_old and du_old required");
+    REQUIRE_ARG(p->vxyz.stride == p->axyz.stride, "vxyz and axyz must share one element stride");
+    LocalFields lf{p->xyz.x,  p->xyz.y,  p->xyz.z,  p->vxyz.x, p->vxyz.y,  p->vxyz.z,
+                   p->axyz.x, p->axyz.y, p->axyz.z, p->vxyz.stride, p->hpart, p->uint, p->duint};
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    { k_reset_corrector<<<1, 1, 0, c.stream>>>(dsc); GBSPH_COUNTED; }
+    CU(kdk_correct64(c, lf, p->n, a_old.x, a_old.y, a_old.z, a_old.stride, du_old, dt));
+    CU(sync_scalars(c));
+    f64 veps  = std::sqrt(ordered_to_f64(c.h_scalars->epsv2_max));
+    f64 vmean = std::sqrt(c.h_scalars->sum_v2 / f64(p->n));
+    f64 eps_v = veps / vmean;
+    if (vmean <= 0) eps_v = 0;
+    if (eps_v_host) *eps_v_host = eps_v;
+    return GBSPH_OK;
+}
+
+int gbsph_cfl(gbsph_ctx *ctx, const double *h, const double *vsig, gbsph_vec3 a, uint32_t n,
+              double C_cour, double C_force, double *dt_part, double *dt_min_host, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(h && vsig && a.x && a.y && a.z, "h, vsig and a required");
+    REQUIRE_ARG(n > 0, "empty patch");
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    { k_reset_corrector<<<1, 1, 0, c.stream>>>(dsc); GBSPH_COUNTED; }
+    CU(cfl64(c, n, h, vsig, a.x, a.y, a.z, a.stride, C_cour, C_force, dt_part));
+    CU(sync_scalars(c));
+    if (dt_min_host) *dt_min_host = ordered_to_f64(c.h_scalars->dt_min);
+    return GBSPH_OK;
+}
+
 int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
                          const uint32_t *entries, const double *x, const double *y,
                          const double *z, const double *vx, const double *vy, const double *vz,

@@ -431,6 +431,69 @@ cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 
     { k_derivs_step<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, lf, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
+// leapfrog corrector (integrators.cpp:88-120): v += dt/2 (a_new - a_old), u likewise;
+// max |dv|^2 and sum |v|^2 for the eps_v rerun test (Solver.cpp:2580-2616)
+__global__ void k_kdk_correct(LocalFields lf, u32 n, const f64 *__restrict__ aox,
+                              const f64 *__restrict__ aoy, const f64 *__restrict__ aoz, u32 avs,
+                              const f64 *__restrict__ du_old, f64 hdt, Scalars *sc) {
+    u32 i   = blockIdx.x * blockDim.x + threadIdx.x;
+    u64 ev2 = 0;
+    f64 v2  = 0;
+    if (i < n) {
+        size_t iv = (size_t) i * lf.vs, io = (size_t) i * avs;
+        f64 ix = hdt * (lf.ax[iv] - aox[io]);
+        f64 iy = hdt * (lf.ay[iv] - aoy[io]);
+        f64 iz = hdt * (lf.az[iv] - aoz[io]);
+        f64 vx = lf.vx[iv] + ix, vy = lf.vy[iv] + iy, vz = lf.vz[iv] + iz;
+        lf.vx[iv] = vx;
+        lf.vy[iv] = vy;
+        lf.vz[iv] = vz;
+        lf.u[i]   = lf.u[i] + hdt * (lf.du[i] - du_old[i]);
+        ev2       = f64_to_ordered(__dadd_rn(__dadd_rn(ix * ix, iy * iy), iz * iz));
+        v2        = __dadd_rn(__dadd_rn(vx * vx, vy * vy), vz * vz);
+    }
+    ev2 = block_reduce(ev2, OpMaxU64{}, 0ull);
+    v2  = block_reduce(v2, OpAddF64{}, 0.0);
+    if (threadIdx.x == 0) {
+        atomicMax((unsigned long long *) &sc->epsv2_max, (unsigned long long) ev2);
+        atomicAdd(&sc->sum_v2, v2);
+    }
+}
+
+// CFL (ComputeCFLCourant.hpp:45-60, ComputeCFLForce.hpp:50-62) and its minimum
+__global__ void k_cfl(u32 n, const f64 *__restrict__ h, const f64 *__restrict__ vsig,
+                      const f64 *__restrict__ ax, const f64 *__restrict__ ay,
+                      const f64 *__restrict__ az, u32 avs, f64 C_cour, f64 C_force,
+                      f64 *__restrict__ dt_part, Scalars *sc) {
+    u32 i   = blockIdx.x * blockDim.x + threadIdx.x;
+    u64 dtm = ~0ull;
+    if (i < n) {
+        size_t io = (size_t) i * avs;
+        f64 dt    = __longlong_as_double(0x7ff0000000000000ll);
+        dt        = fmin(dt, C_cour * h[i] / vsig[i]);
+        f64 a0 = ax[io], a1 = ay[io], a2 = az[io];
+        f64 abs_a = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+        dt        = fmin(dt, C_force * sqrt(h[i] / abs_a));
+        if (dt_part) dt_part[i] = dt;
+        dtm = f64_to_ordered(dt);
+    }
+    dtm = block_reduce(dtm, OpMinU64{}, ~0ull);
+    if (threadIdx.x == 0) atomicMin((unsigned long long *) &sc->dt_min, (unsigned long long) dtm);
+}
+
+cudaError_t kdk_correct64(Ctx &c, const LocalFields &lf, u32 n, const f64 *aox, const f64 *aoy,
+                          const f64 *aoz, u32 avs, const f64 *du_old, f64 dt) {
+    { k_kdk_correct<<<div_up(n, 256), 256, 0, c.stream>>>(lf, n, aox, aoy, aoz, avs, du_old, dt / 2,
+                                                         c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t cfl64(Ctx &c, u32 n, const f64 *h, const f64 *vsig, const f64 *ax, const f64 *ay,
+                  const f64 *az, u32 avs, f64 C_cour, f64 C_force, f64 *dt_part) {
+    { k_cfl<<<div_up(n, 256), 256, 0, c.stream>>>(n, h, vsig, ax, ay, az, avs, C_cour, C_force,
+                                                 dt_part, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
 cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic, const f64 *bmin,
                       const f64 *bmax) {
     ProfScope ps(c, kProfPredict, n);

@@ -56,6 +56,10 @@ cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 
                           const LocalFields &lf);
 cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic, const f64 *bmin,
                       const f64 *bmax);
+cudaError_t kdk_correct64(Ctx &c, const LocalFields &lf, u32 n, const f64 *aox, const f64 *aoy,
+                          const f64 *aoz, u32 avs, const f64 *du_old, f64 dt);
+cudaError_t cfl64(Ctx &c, u32 n, const f64 *h, const f64 *vsig, const f64 *ax, const f64 *ay,
+                  const f64 *az, u32 avs, f64 C_cour, f64 C_force, f64 *dt_part);
 cudaError_t scatter_rows(Ctx &c, u32 n, const f64 *src, f64 *dst);
 cudaError_t gather_rows(Ctx &c, u32 n, const f64 *src_rank, f64 *dst, f64 *dst2);
 cudaError_t fill64(Ctx &c, u32 n, f64 *dst, f64 v);

@@ -197,3 +197,49 @@ def periodic_ghosts(ctx, pos, h, bmin, bmax, htol):
     ctx.call("gbsph_ghost_export", _p(src), _p(oid), _p(m[0]), _p(m[1]), _p(m[2]), _p(m[3]), None)
     return dict(src=src[:G].cpu().numpy().view(np.uint32), offset_id=oid[:G].cpu().numpy(),
                 merged_pos=m[:3].T.cpu().numpy(), merged_h=m[3].cpu().numpy())
+
+
+def _vec3(t):
+    return L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0)
+
+
+def _particles(x, v, a, h, u, du):
+    p = L.Particles()
+    p.n = h.shape[0]
+    p.xyz, p.vxyz, p.axyz = _vec3(x), _vec3(v), _vec3(a)
+    p.hpart, p.uint, p.duint = h.data_ptr(), u.data_ptr(), du.data_ptr()
+    p.omega = None
+    return p
+
+
+def kdk_predict(ctx, pos, v, u, a, du, dt, periodic=False, bmin=(0, 0, 0), bmax=(1, 1, 1)):
+    """Leapfrog predictor + periodic wrap; returns new (pos (3, N), v (3, N), u)."""
+    x, vv, aa = soa(pos).clone(), soa(v).clone(), soa(a)
+    uu, dd = _cuda(u, torch.float64).clone(), _cuda(du, torch.float64)
+    h = torch.zeros_like(uu)
+    p = _particles(x, vv, aa, h, uu, dd)
+    ctx.call("gbsph_kdk_predict", C.byref(p), dt, 1 if periodic else 0, L.d3(bmin), L.d3(bmax), None)
+    return x, vv, uu
+
+
+def kdk_correct(ctx, v, u, a_new, a_old, du_new, du_old, dt):
+    """Leapfrog corrector; returns new (v (3, N), u) and eps_v."""
+    vv, aa, ao = soa(v).clone(), soa(a_new), soa(a_old)
+    uu, dd, do = (_cuda(t, torch.float64) for t in (u, du_new, du_old))
+    uu = uu.clone()
+    x = torch.zeros_like(vv)
+    h = torch.zeros_like(uu)
+    p = _particles(x, vv, aa, h, uu, dd)
+    e = C.c_double()
+    ctx.call("gbsph_kdk_correct", C.byref(p), _vec3(ao), _p(do), dt, C.byref(e), None)
+    return vv, uu, e.value
+
+
+def cfl(ctx, h, vsig, a, C_cour, C_force):
+    """Per-particle CFL dt and its minimum."""
+    h, vs, aa = _cuda(h, torch.float64), _cuda(vsig, torch.float64), soa(a)
+    dtp = torch.empty_like(h)
+    m = C.c_double()
+    ctx.call("gbsph_cfl", _p(h), _p(vs), _vec3(aa), h.shape[0], C_cour, C_force, _p(dtp),
+             C.byref(m), None)
+    return m.value, dtp

@@ -157,3 +157,40 @@ def test_derivs_mixed_within_tolerance(gctx, M, scene):
     ed = rel_err(du32.cpu().numpy(), du64.cpu().numpy())
     ev = rel_err(vs32.cpu().numpy(), vs64.cpu().numpy())
     assert ea[0] <= tol and ed[0] <= tol and ev[0] <= tol, (ea, ed, ev)
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_kdk_predict_vs_oracle(gctx, periodic):
+    from shamrock_gb300 import modules as M
+
+    rng = np.random.default_rng(21)
+    n = 3000
+    pos = rng.random((n, 3))
+    v, a = rng.normal(0, 0.3, (n, 3)), rng.normal(0, 2.0, (n, 3))
+    u, du = rng.uniform(0.5, 1.5, n), rng.normal(0, 1.0, n)
+    dt = 0.037
+    x, vv, uu = M.kdk_predict(gctx, pos, v, u, a, du, dt, periodic, (0, 0, 0), (1, 1, 1))
+    ox, ov, ou = O.predict(pos, v, u, a, du, dt, periodic, [0, 0, 0], [1, 1, 1])
+    assert np.array_equal(x.T.cpu().numpy(), ox)
+    assert np.array_equal(vv.T.cpu().numpy(), ov)
+    assert np.array_equal(uu.cpu().numpy(), ou)
+
+
+def test_kdk_correct_and_cfl_vs_oracle(gctx):
+    from shamrock_gb300 import modules as M
+
+    rng = np.random.default_rng(22)
+    n = 5000
+    v, a_new, a_old = (rng.normal(0, s, (n, 3)) for s in (0.3, 2.0, 2.0))
+    u, du_new, du_old = rng.uniform(0.5, 1.5, n), rng.normal(0, 1, n), rng.normal(0, 1, n)
+    dt = 0.011
+    vv, uu, e = M.kdk_correct(gctx, v, u, a_new, a_old, du_new, du_old, dt)
+    ov, ou, oe = O.correct(v, u, a_new, a_old, du_new, du_old, dt)
+    assert np.array_equal(vv.T.cpu().numpy(), ov)
+    assert np.array_equal(uu.cpu().numpy(), ou)
+    assert abs(e - oe) <= 1e-12 * oe  # sum of v^2 reduced in another order
+    h, vsig = rng.uniform(0.01, 0.05, n), rng.uniform(0.5, 3.0, n)
+    m, dtp = M.cfl(gctx, h, vsig, a_new, 0.3, 0.25)
+    om, odtp = O.cfl(h, vsig, a_new, 0.3, 0.25)
+    assert m == om
+    assert np.array_equal(dtp.cpu().numpy(), odtp)
