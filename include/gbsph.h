@@ -81,7 +81,23 @@ typedef struct {
      * that).  Smaller values converge h further, e.g. for finite-difference checks of
      * the adjoint, which differentiates h as the exact root of the density constraint. */
     double epsilon_h_particle;
+    /* Equation of state: GBSPH_EOS_ADIABATIC (gamma) or GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07,
+     * c_s^2 = cs0^2 (R^2 / r0^2)^(-q) at the particle's position R, P = c_s^2 rho
+     * (SolverConfig EOSConfig::LocallyIsothermalLP07, ComputeEos.cpp:725-798). */
+    uint32_t eos_kind;
+    /* External force: GBSPH_EXT_NONE or GBSPH_EXT_POINT_MASS, a central mass at the origin,
+     * a = -G M r / |r|^3, evaluated after the drift and added to the hydro acceleration
+     * (ExtForceConfig::PointMass, AddForceCentralGravPotential.cpp:37-48), without
+     * accretion. */
+    uint32_t ext_kind;
+    double cs0, eos_r0, eos_q;
+    double central_mass, constant_G;
 } gbsph_config;
+
+#define GBSPH_EOS_ADIABATIC 0
+#define GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07 1
+#define GBSPH_EXT_NONE 0
+#define GBSPH_EXT_POINT_MASS 1
 
 /* Synchronised solver state (the scheduler edges "time", "dt", "cfl_multiplier",
  * shammodels/sph/include/shammodels/sph/Solver.hpp:99-145). */
@@ -187,6 +203,12 @@ int gbsph_h_iterate(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned
 int gbsph_omega(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
                 const uint32_t *entries, const double *x, const double *y, const double *z,
                 const double *h, uint32_t n_local, double pmass, double *omega, void *stream);
+
+/* Locally isothermal EOS, LP07 (ComputeEos.cpp:725-798, shamphys/eos.hpp:87-98):
+ * c_s^2 = cs0^2 (R^2 / r0^2)^(-q) at the position R, P = c_s^2 rho_h(m, h). */
+int gbsph_eos_locally_isothermal(gbsph_ctx *ctx, gbsph_vec3 xyz, const double *h, uint32_t n,
+                                 double pmass, double cs0, double r0, double q, double *P,
+                                 double *cs, void *stream);
 
 /* ComputeEOSAdiabatic from h, shammodels/sph/src/modules/ComputeEos.cpp:153-245. */
 int gbsph_eos_adiabatic(gbsph_ctx *ctx, const double *h, const double *u, uint32_t n, double pmass,

@@ -677,6 +677,39 @@ void eos_adiabatic(u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamma, f64 
     }
 }
 
+// Locally isothermal EOS (LP07) — shammodels/sph/src/modules/ComputeEos.cpp:725-798,
+// shamphys/include/shamphys/eos.hpp:87-98: c_s^2 = cs0^2 (R^2 / r0^2)^(-q) at the merged
+// position R, P = c_s^2 rho.
+void eos_locally_isothermal(u32 n, const f64 *xyz, const f64 *h, f64 pmass, f64 cs0, f64 r0,
+                            f64 q, f64 *P, f64 *cs) {
+    const f64 r0sq = r0 * r0, mq = -q;
+#pragma omp parallel for schedule(static)
+    for (i64 i = 0; i < (i64) n; i++) {
+        f64 x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        f64 Rsq   = x * x + y * y + z * z;
+        f64 cs_sq = (cs0 * cs0) * std::pow(Rsq / r0sq, mq);
+        f64 rho   = rho_h(pmass, h[i], hfactd);
+        P[i]      = cs_sq * rho;
+        cs[i]     = std::sqrt(cs_sq);
+    }
+}
+
+// Central point mass at the origin — shammodels/common/src/modules/AddForceCentralGravPotential.cpp:37-48:
+// a_ext = (-M G) r / |r|^3, evaluated after the predictor's drift (ExternalForces.cpp,
+// compute_ext_forces_indep_v, called from Solver.cpp:2035) and added to the hydro
+// acceleration of every corrector evaluation (ExternalForces.cpp:342-359).
+void point_mass_accel(u32 n, const f64 *xyz, f64 central_mass, f64 G, f64 *aext) {
+    const f64 mGM = -central_mass * G;
+    for (u32 i = 0; i < n; i++) {
+        f64 x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        f64 r   = std::sqrt(x * x + y * y + z * z);
+        f64 r3  = r * r * r;
+        aext[3 * i]     = mGM * x / r3;
+        aext[3 * i + 1] = mGM * y / r3;
+        aext[3 * i + 2] = mGM * z / r3;
+    }
+}
+
 inline f64 inv_sat_positive(f64 v) { return (v >= 1e-9) ? 1. / v : 0.; }
 inline f64 inv_sat_zero(f64 v) { return (v != 0 && v == v) ? 1. / v : 0.; }
 
@@ -809,7 +842,8 @@ f64 cfl_min(u32 n, const f64 *h, const f64 *vsig, const f64 *axyz, f64 C_cour, f
 // v += dt/2 a, u += dt/2 du (half step 1), x += dt v, then the second half step, and the
 // periodic wrap of the positions (integrators.cpp:207-237).
 void leapfrog_predict(u32 n, f64 *xyz, f64 *vxyz, f64 *u, const f64 *axyz, const f64 *du, f64 dt,
-                      u32 periodic, const f64 *bmin, const f64 *bmax) {
+                      u32 periodic, const f64 *bmin, const f64 *bmax, f64 *aext_out = nullptr,
+                      f64 central_mass = 0, f64 G = 0) {
     const f64 dt_half = dt / 2;
     for (u32 i = 0; i < n; i++) {
         for (int c = 0; c < 3; c++) vxyz[3 * i + c] = vxyz[3 * i + c] + dt_half * axyz[3 * i + c];
@@ -820,6 +854,8 @@ void leapfrog_predict(u32 n, f64 *xyz, f64 *vxyz, f64 *u, const f64 *axyz, const
         for (int c = 0; c < 3; c++) vxyz[3 * i + c] = vxyz[3 * i + c] + dt_half * axyz[3 * i + c];
         u[i] = u[i] + dt_half * du[i];
     }
+    // velocity-independent external forces at the drifted positions, before the wrap
+    if (aext_out) point_mass_accel(n, xyz, central_mass, G, aext_out);
     if (periodic) {
         for (u32 i = 0; i < n; i++)
             for (int c = 0; c < 3; c++) {
@@ -924,6 +960,10 @@ struct Config {
     u32 tree_reduction_level;
     u32 periodic;
     f64 bmin[3], bmax[3];
+    u32 eos_kind; // 0 adiabatic, 1 locally isothermal (LP07)
+    u32 ext_kind; // 0 none, 1 central point mass
+    f64 cs0, eos_r0, eos_q;        // LP07: c_s^2 = cs0^2 (R^2 / r0^2)^(-q)
+    f64 central_mass, constant_G;  // point mass at the origin
 };
 
 struct StepLog {
@@ -977,8 +1017,11 @@ void evolve_once(Sim &s, StepLog &log) {
     log.dt            = dt;
     log.n_local       = n;
 
+    std::vector<f64> aext;
+    if (cfg.ext_kind == 1) aext.assign(3 * (size_t) n, 0);
     leapfrog_predict(n, s.xyz.data(), s.vxyz.data(), s.u.data(), s.axyz.data(), s.du.data(), dt,
-                     cfg.periodic, cfg.bmin, cfg.bmax);
+                     cfg.periodic, cfg.bmin, cfg.bmax, cfg.ext_kind == 1 ? aext.data() : nullptr,
+                     cfg.central_mass, cfg.constant_G);
 
     // sph_prestep
     std::vector<f64> mxyz, mh;
@@ -1051,12 +1094,18 @@ void evolve_once(Sim &s, StepLog &log) {
         u32 N = (u32) m_h.size();
         s.P.assign(N, 0);
         s.cs.assign(N, 0);
-        eos_adiabatic(N, m_h.data(), m_u.data(), cfg.pmass, cfg.gamma, s.P.data(), s.cs.data());
+        if (cfg.eos_kind == 1)
+            eos_locally_isothermal(N, mxyz.data(), m_h.data(), cfg.pmass, cfg.cs0, cfg.eos_r0,
+                                   cfg.eos_q, s.P.data(), s.cs.data());
+        else
+            eos_adiabatic(N, m_h.data(), m_u.data(), cfg.pmass, cfg.gamma, s.P.data(), s.cs.data());
         std::vector<f64> old_a(s.axyz), old_du(s.du);
         derivs_constAV(n, s.cache.part.cnt.data(), s.cache.part.scanned.data(),
                        s.cache.part.entries.data(), mxyz.data(), m_v.data(), m_h.data(),
                        m_om.data(), m_u.data(), s.P.data(), s.cs.data(), cfg.pmass, cfg.alpha_u,
                        cfg.alpha_AV, cfg.beta_AV, s.axyz.data(), s.du.data());
+        if (cfg.ext_kind == 1)
+            for (size_t k = 0; k < 3 * (size_t) n; k++) s.axyz[k] = s.axyz[k] + aext[k];
         f64 eps_v = leapfrog_correct(n, s.vxyz.data(), s.u.data(), s.axyz.data(), old_a.data(),
                                      s.du.data(), old_du.data(), dt);
         log.eps_v = eps_v;
@@ -1232,6 +1281,10 @@ void orc_h_iterate_once(u32 n, const u32 *cnt, const u32 *sc, const u32 *ent, co
 void orc_omega(u32 n, const u32 *cnt, const u32 *sc, const u32 *ent, const f64 *r, const f64 *h,
                f64 pmass, f64 *omega) {
     orc::compute_omega(n, cnt, sc, ent, r, h, pmass, omega);
+}
+void orc_eos_locally_isothermal(u32 n, const f64 *xyz, const f64 *h, f64 pmass, f64 cs0, f64 r0,
+                                f64 q, f64 *P, f64 *cs) {
+    orc::eos_locally_isothermal(n, xyz, h, pmass, cs0, r0, q, P, cs);
 }
 void orc_eos_adiabatic(u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamma, f64 *P, f64 *cs) {
     orc::eos_adiabatic(n, h, u, pmass, gamma, P, cs);

@@ -33,6 +33,9 @@ class OrcConfig(C.Structure):
         ("h_iter_per_subcycles", C.c_uint32), ("h_max_subcycles", C.c_uint32),
         ("tree_reduction_level", C.c_uint32), ("periodic", C.c_uint32),
         ("bmin", C.c_double * 3), ("bmax", C.c_double * 3),
+        ("eos_kind", C.c_uint32), ("ext_kind", C.c_uint32),
+        ("cs0", C.c_double), ("eos_r0", C.c_double), ("eos_q", C.c_double),
+        ("central_mass", C.c_double), ("constant_G", C.c_double),
     ]
 
 
@@ -100,6 +103,8 @@ def lib():
                                       C.c_double, _f64p, _f64p]),
         "orc_vsig": (None, [C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p, _f64p, _f64p]),
         "orc_cfl": (C.c_double, [C.c_uint32, _f64p, _f64p, _f64p, C.c_double, C.c_double, _vp]),
+        "orc_eos_locally_isothermal": (None, [C.c_uint32, _f64p, _f64p, C.c_double, C.c_double,
+                                              C.c_double, C.c_double, _f64p, _f64p]),
         "orc_predict": (None, [C.c_uint32, _f64p, _f64p, _f64p, _f64p, _f64p, C.c_double,
                                C.c_uint32, _f64p, _f64p]),
         "orc_correct": (C.c_double, [C.c_uint32, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p,
@@ -296,6 +301,13 @@ def cfl(h, vsig_, a, C_cour, C_force):
     dtp = np.zeros(len(h))
     m = lib().orc_cfl(len(h), h, _f64(vsig_), _f64(a, (-1, 3)), C_cour, C_force, _ptr(dtp))
     return m, dtp
+
+
+def eos_locally_isothermal(pos, h, pmass, cs0, r0, q):
+    h = _f64(h)
+    P, cs = np.zeros(len(h)), np.zeros(len(h))
+    lib().orc_eos_locally_isothermal(len(h), _f64(pos, (-1, 3)), h, pmass, cs0, r0, q, P, cs)
+    return P, cs
 
 
 def predict(pos, v, u, a, du, dt, periodic, bmin, bmax):

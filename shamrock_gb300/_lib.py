@@ -42,7 +42,9 @@ class Config(C.Structure):
                 ("epsilon_h", _f64), ("h_iter_per_subcycles", _u32), ("h_max_subcycles", _u32),
                 ("tree_reduction_level", _u32), ("periodic", _u32), ("box_min", _d3),
                 ("box_max", _d3), ("precision", _u32), ("pad", _u32),
-                ("epsilon_h_particle", _f64)]
+                ("epsilon_h_particle", _f64), ("eos_kind", _u32), ("ext_kind", _u32),
+                ("cs0", _f64), ("eos_r0", _f64), ("eos_q", _f64), ("central_mass", _f64),
+                ("constant_G", _f64)]
 
 
 class TimeState(C.Structure):
@@ -86,6 +88,8 @@ SIGNATURES = {
                                   _f64, _f64, _u32, _P(_f64), _P(_f64), _P(_u32), _vp]),
     "gbsph_omega": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u32, _f64, _vp, _vp]),
     "gbsph_eos_adiabatic": (C.c_int, [_vp, _vp, _vp, _u32, _f64, _f64, _vp, _vp, _vp]),
+    "gbsph_eos_locally_isothermal": (C.c_int, [_vp, Vec3, _vp, _u32, _f64, _f64, _f64, _f64, _vp,
+                                               _vp, _vp]),
     "gbsph_derivs_constAV": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _vp, _vp, _vp, _u32, _u32, _f64, _f64, _f64, _f64,
                                        _u32, _vp, _vp, _vp, _vp, _vp, _vp]),

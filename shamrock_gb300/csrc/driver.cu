@@ -64,7 +64,7 @@ Ctx::~Ctx() {
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
                       &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
-                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank};
+                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &aext};
     cudaSetDevice(device);
     for (DevBuf *b : bufs) b->release(stream);
     cudaStreamSynchronize(stream);
@@ -500,6 +500,18 @@ int gbsph_cfl(gbsph_ctx *ctx, const double *h, const double *vsig, gbsph_vec3 a,
     return GBSPH_OK;
 }
 
+int gbsph_eos_locally_isothermal(gbsph_ctx *ctx, gbsph_vec3 xyz, const double *h, uint32_t n,
+                                 double pmass, double cs0, double r0, double q, double *P,
+                                 double *cs, void *stream) {
+    ENTER(ctx, stream);
+    REQUIRE_ARG(xyz.x && xyz.y && xyz.z && h && P && cs, "null argument");
+    REQUIRE_ARG(r0 > 0, "r0 must be positive");
+    if (n == 0) return GBSPH_OK;
+    CU(eos_lp07(ctx->c, n, xyz.x, xyz.y, xyz.z, xyz.stride, h, pmass, cs0, r0, q, P, cs));
+    CU(cudaStreamSynchronize(ctx->c.stream));
+    return GBSPH_OK;
+}
+
 int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *scanned,
                          const uint32_t *entries, const double *x, const double *y,
                          const double *z, const double *vx, const double *vy, const double *vz,
@@ -568,6 +580,12 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     REQUIRE_ARG(cfg->precision == GBSPH_FP64 || cfg->precision == GBSPH_MIXED, "unknown precision");
     REQUIRE_ARG(p->xyz.stride == p->vxyz.stride && p->xyz.stride == p->axyz.stride,
                 "xyz, vxyz and axyz must share one element stride");
+    REQUIRE_ARG(cfg->eos_kind == GBSPH_EOS_ADIABATIC || cfg->eos_kind == GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07,
+                "unknown equation of state");
+    REQUIRE_ARG(cfg->ext_kind == GBSPH_EXT_NONE || cfg->ext_kind == GBSPH_EXT_POINT_MASS,
+                "unknown external force");
+    REQUIRE_ARG(cfg->eos_kind != GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07 || cfg->eos_r0 > 0,
+                "locally isothermal EOS needs r0 > 0");
     auto t_start = std::chrono::steady_clock::now();
     cudaStream_t s = c.stream;
     const u32 n    = p->n;
@@ -583,8 +601,18 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     Scalars *dsc = c.d_scalars.as<Scalars>();
     CU(cudaMemsetAsync(dsc, 0, sizeof(Scalars), s));
 
-    // ---- leapfrog predictor + position boundary
-    CU(predict64(c, lf, n, dt, (int) cfg->periodic, cfg->box_min, cfg->box_max));
+    // ---- leapfrog predictor + position boundary (+ velocity-independent external force)
+    ExtAccel ext{nullptr, nullptr, nullptr};
+    if (cfg->ext_kind == GBSPH_EXT_POINT_MASS) {
+        CU(c.aext.ensure(sizeof(f64) * 3 * (size_t) n, s));
+        f64 *A = c.aext.as<f64>();
+        ext    = ExtAccel{A, A + n, A + 2 * (size_t) n};
+        CU(predict64(c, lf, n, dt, (int) cfg->periodic, cfg->box_min, cfg->box_max,
+                     -cfg->central_mass * cfg->constant_G, A, A + n, A + 2 * (size_t) n));
+    } else {
+        CU(predict64(c, lf, n, dt, (int) cfg->periodic, cfg->box_min, cfg->box_max));
+    }
+    const EosParams eos{cfg->eos_kind, cfg->gamma, cfg->cs0, cfg->eos_r0, cfg->eos_q};
 
     // ---- sph_prestep (Solver.cpp:1060-1304)
     CU(c.h_old_row.ensure(8 * (size_t) n, s));
@@ -692,7 +720,7 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             return fail(ctx, GBSPH_ERR_NOT_CONVERGED,
                         "the corrector has made over 50 loops, either their is a bug, either you "
                         "are using a dt that is too large");
-        CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, cfg->gamma));
+        CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
         if (tape) {
             { k_snap_vu<<<div_up(n, 256), 256, 0, s>>>(
                 n, lf.vx, lf.vy, lf.vz, lf.vs, lf.u,
@@ -704,10 +732,10 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
         if (mixed)
             CU(derivs_step_mixed(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
-                                 dt / 2, C_cour, C_force, lf));
+                                 dt / 2, C_cour, C_force, lf, ext));
         else
             CU(derivs_step64(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
-                             dt / 2, C_cour, C_force, lf));
+                             dt / 2, C_cour, C_force, lf, ext));
         CU(sync_scalars(c));
         f64 rank_veps_v = std::sqrt(ordered_to_f64(c.h_scalars->epsv2_max));
         f64 vmean       = std::sqrt(c.h_scalars->sum_v2 / f64(n));
@@ -766,6 +794,8 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     REQUIRE_ARG(cot->gx.stride == cot->gv.stride && cot->gx.stride == cot->ga.stride,
                 "gx, gv and ga must share one element stride");
     REQUIRE_ARG(dt >= 0, "dt must be the forward step's dt");
+    REQUIRE_ARG(cfg->eos_kind == GBSPH_EOS_ADIABATIC && cfg->ext_kind == GBSPH_EXT_NONE,
+                "the adjoint covers the adiabatic EOS without external forces");
     cudaStream_t s = c.stream;
     const u32 n    = start->n;
     // recompute the step on a working copy of the start state

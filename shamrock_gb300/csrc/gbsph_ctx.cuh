@@ -137,6 +137,7 @@ struct Ctx {
 
     // ---- per-row / per-local work arrays
     DevBuf h_old_row, eps_row, omega_local, a_old, du_old, hnew_row, omega_row;
+    DevBuf aext; // external acceleration of the step (3 n, SoA)
     DevBuf dt_part;
 
     // ---- adjoint: working state, tape, accumulators (local and rank order)

@@ -145,7 +145,9 @@ __global__ void k_gather_eos(const u32 *__restrict__ sort_index, u32 N, u32 n_lo
                              const u32 *__restrict__ ghost_src, const f64 *__restrict__ h,
                              const f64 *__restrict__ u, const f64 *__restrict__ vx,
                              const f64 *__restrict__ vy, const f64 *__restrict__ vz, u32 vs,
-                             const f64 *__restrict__ omega, f64 pmass, f64 gamma,
+                             const f64 *__restrict__ omega, f64 pmass, EosParams eos,
+                             const f64 *__restrict__ sx, const f64 *__restrict__ sy,
+                             const f64 *__restrict__ sz,
                              f64 *__restrict__ sh, f64 *__restrict__ su, f64 *__restrict__ svx,
                              f64 *__restrict__ svy, f64 *__restrict__ svz, f64 *__restrict__ som,
                              f64 *__restrict__ sP, f64 *__restrict__ scs) {
@@ -161,9 +163,31 @@ __global__ void k_gather_eos(const u32 *__restrict__ sort_index, u32 N, u32 n_lo
     svz[r] = vz[(size_t) src * vs];
     som[r] = omega[src];
     f64 rho = rho_h(pmass, hh);
-    f64 P   = (gamma - 1) * rho * uu;
-    sP[r]   = P;
-    scs[r]  = sqrt(gamma * P / rho);
+    if (eos.kind == 1) {
+        // LP07 at the merged (rank-ordered) position
+        f64 x = sx[r], y = sy[r], z = sz[r];
+        f64 Rsq   = x * x + y * y + z * z;
+        f64 cs_sq = (eos.cs0 * eos.cs0) * pow(Rsq / (eos.r0 * eos.r0), -eos.q);
+        sP[r]     = cs_sq * rho;
+        scs[r]    = sqrt(cs_sq);
+    } else {
+        f64 P  = (eos.gamma - 1) * rho * uu;
+        sP[r]  = P;
+        scs[r] = sqrt(eos.gamma * P / rho);
+    }
+}
+
+__global__ void k_eos_lp07(u32 n, const f64 *__restrict__ x, const f64 *__restrict__ y,
+                           const f64 *__restrict__ z, u32 vs, const f64 *__restrict__ h, f64 pmass,
+                           f64 cs0, f64 r0, f64 q, f64 *__restrict__ P, f64 *__restrict__ cs) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t iv = (size_t) i * vs;
+    f64 a = x[iv], b = y[iv], c = z[iv];
+    f64 Rsq   = a * a + b * b + c * c;
+    f64 cs_sq = (cs0 * cs0) * pow(Rsq / (r0 * r0), -q);
+    P[i]      = cs_sq * rho_h(pmass, h[i]);
+    cs[i]     = sqrt(cs_sq);
 }
 
 __global__ void k_eos(u32 n, const f64 *__restrict__ h, const f64 *__restrict__ u, f64 pmass,
@@ -181,6 +205,7 @@ struct DerivParams {
     f64 pmass, alpha_u, alpha_AV, beta_AV;
     f64 hdt;             // dt / 2 for the corrector
     f64 C_cour, C_force; // CFL factors (already x cfl multiplier)
+    ExtAccel ext;        // external acceleration added to the hydro one (may be null)
 };
 
 template<bool VSIG>
@@ -289,6 +314,12 @@ __global__ void __launch_bounds__(128) k_derivs_step(RowSpace rs, HydroSpace hs,
         derivs_row<true>(rs, hs, a, k0, k1, p, fx, fy, fz, tdu, vm);
         u32 i  = rs.row_local[t];
         size_t iv = (size_t) i * lf.vs;
+        if (p.ext.x) {
+            // axyz += axyz_ext (ExternalForces.cpp:342-359)
+            fx = fx + p.ext.x[i];
+            fy = fy + p.ext.y[i];
+            fz = fz + p.ext.z[i];
+        }
         f64 ox = lf.ax[iv], oy = lf.ay[iv], oz = lf.az[iv], odu = lf.du[i];
         lf.ax[iv] = fx;
         lf.ay[iv] = fy;
@@ -326,7 +357,8 @@ __global__ void __launch_bounds__(128) k_derivs_step(RowSpace rs, HydroSpace hs,
 
 // leapfrog predictor (half kick, drift, half kick) + periodic wrap, one pass
 __global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f64 b1, f64 b2,
-                          f64 e0, f64 e1, f64 e2) {
+                          f64 e0, f64 e1, f64 e2, f64 mGM, f64 *__restrict__ ext_x,
+                          f64 *__restrict__ ext_y, f64 *__restrict__ ext_z) {
     u32 i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     size_t iv   = (size_t) i * lf.vs;
@@ -342,6 +374,14 @@ __global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f
     vy = vy + dt_half * ay;
     vz = vz + dt_half * az;
     u  = u + dt_half * dd;
+    if (ext_x) {
+        // central point mass at the drifted position, before the wrap
+        f64 r  = sqrt(x * x + y * y + z * z);
+        f64 r3 = r * r * r;
+        ext_x[i] = mGM * x / r3;
+        ext_y[i] = mGM * y / r3;
+        ext_z[i] = mGM * z / r3;
+    }
     if (periodic) {
         f64 bmin[3] = {b0, b1, b2}, bmax[3] = {e0, e1, e2};
         f64 p[3]    = {x, y, z};
@@ -409,24 +449,30 @@ cudaError_t eos64(Ctx &c, u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamm
     return cudaGetLastError();
 }
 cudaError_t gather_eos64(Ctx &c, u32 N, u32 n_local, const LocalFields &lf, const f64 *omega_local,
-                         f64 pmass, f64 gamma) {
+                         f64 pmass, const EosParams &eos) {
     ProfScope ps(c, kProfGatherEos, N);
     { k_gather_eos<<<div_up(N, 256), 256, 0, c.stream>>>(
         c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf.h, lf.u, lf.vx, lf.vy, lf.vz,
-        lf.vs, omega_local, pmass, gamma, c.sh2.as<f64>(), c.su.as<f64>(), c.svx.as<f64>(),
-        c.svy.as<f64>(), c.svz.as<f64>(), c.som.as<f64>(), c.sP.as<f64>(), c.scs.as<f64>()); GBSPH_COUNTED; }
+        lf.vs, omega_local, pmass, eos, c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
+        c.sh2.as<f64>(), c.su.as<f64>(), c.svx.as<f64>(), c.svy.as<f64>(), c.svz.as<f64>(),
+        c.som.as<f64>(), c.sP.as<f64>(), c.scs.as<f64>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t eos_lp07(Ctx &c, u32 n, const f64 *x, const f64 *y, const f64 *z, u32 vs, const f64 *h,
+                     f64 pmass, f64 cs0, f64 r0, f64 q, f64 *P, f64 *cs) {
+    { k_eos_lp07<<<div_up(n, 256), 256, 0, c.stream>>>(n, x, y, z, vs, h, pmass, cs0, r0, q, P, cs); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t derivs64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
                      f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az, f64 *du, f64 *vsig) {
-    DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, 0, 0, 0};
+    DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, 0, 0, 0, ExtAccel{nullptr, nullptr, nullptr}};
     { k_derivs<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, ax, ay, az, du, vsig); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
                           f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
-                          const LocalFields &lf) {
-    DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, hdt, C_cour, C_force};
+                          const LocalFields &lf, const ExtAccel &ext) {
+    DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, hdt, C_cour, C_force, ext};
     ProfScope ps(c, kProfDerivs, rs.n);
     { k_derivs_step<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, lf, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     return cudaGetLastError();
@@ -495,10 +541,11 @@ cudaError_t cfl64(Ctx &c, u32 n, const f64 *h, const f64 *vsig, const f64 *ax, c
 }
 
 cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic, const f64 *bmin,
-                      const f64 *bmax) {
+                      const f64 *bmax, f64 mGM, f64 *ext_x, f64 *ext_y, f64 *ext_z) {
     ProfScope ps(c, kProfPredict, n);
     { k_predict<<<div_up(n, 256), 256, 0, c.stream>>>(lf, n, dt, periodic, bmin[0], bmin[1], bmin[2],
-                                                   bmax[0], bmax[1], bmax[2]); GBSPH_COUNTED; }
+                                                   bmax[0], bmax[1], bmax[2], mGM, ext_x, ext_y,
+                                                   ext_z); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t scatter_rows(Ctx &c, u32 n, const f64 *src, f64 *dst) {

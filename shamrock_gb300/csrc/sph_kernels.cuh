@@ -28,6 +28,20 @@ struct HydroSpace {
     const f64 *h, *u, *vx, *vy, *vz, *omega, *P, *cs;
 };
 
+// Equation of state of the step: adiabatic (P = (gamma - 1) rho u) or locally
+// isothermal LP07 (c_s^2 = cs0^2 (R^2 / r0^2)^(-q) at the position R, P = c_s^2 rho;
+// shammodels/sph/src/modules/ComputeEos.cpp:725-798).
+struct EosParams {
+    u32 kind; // 0 adiabatic, 1 locally isothermal LP07
+    f64 gamma, cs0, r0, q;
+};
+
+// Velocity-independent external acceleration (local ids, SoA), added to the hydro
+// acceleration of every corrector evaluation; all null when there is none.
+struct ExtAccel {
+    const f64 *x, *y, *z;
+};
+
 // The caller's per-particle arrays (local ids).  Vector components are separate
 // pointers sharing the element stride vs (1 for SoA, 3 or 4 for AoS f64_3).
 struct LocalFields {
@@ -48,14 +62,19 @@ cudaError_t omega64(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64
                     const u32 *out_index);
 cudaError_t eos64(Ctx &c, u32 n, const f64 *h, const f64 *u, f64 pmass, f64 gamma, f64 *P, f64 *cs);
 cudaError_t gather_eos64(Ctx &c, u32 N, u32 n_local, const LocalFields &lf, const f64 *omega_local,
-                         f64 pmass, f64 gamma);
+                         f64 pmass, const EosParams &eos);
+cudaError_t eos_lp07(Ctx &c, u32 n, const f64 *x, const f64 *y, const f64 *z, u32 vs, const f64 *h,
+                     f64 pmass, f64 cs0, f64 r0, f64 q, f64 *P, f64 *cs);
 cudaError_t derivs64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
                      f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az, f64 *du, f64 *vsig);
 cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass, f64 alpha_u,
                           f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
-                          const LocalFields &lf);
+                          const LocalFields &lf, const ExtAccel &ext);
+// mGM != 0: the central point-mass acceleration (-M G) r / |r|^3 at the drifted
+// positions, before the wrap, into ext_out (AddForceCentralGravPotential.cpp:37-48)
 cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic, const f64 *bmin,
-                      const f64 *bmax);
+                      const f64 *bmax, f64 mGM = 0, f64 *ext_x = nullptr, f64 *ext_y = nullptr,
+                      f64 *ext_z = nullptr);
 cudaError_t kdk_correct64(Ctx &c, const LocalFields &lf, u32 n, const f64 *aox, const f64 *aoy,
                           const f64 *aoz, u32 avs, const f64 *du_old, f64 dt);
 cudaError_t cfl64(Ctx &c, u32 n, const f64 *h, const f64 *vsig, const f64 *ax, const f64 *ay,

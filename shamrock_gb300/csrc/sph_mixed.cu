@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
                                                            MixedParams p, f64 pmass,
                                                            const f64 *__restrict__ h_rank, f64 hdt,
                                                            f64 C_cour, f64 C_force, LocalFields lf,
-                                                           Scalars *sc) {
+                                                           ExtAccel ext, Scalars *sc) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     u64 ev2 = 0, dtm = ~0ull;
     f64 v2  = 0;
@@ -331,6 +331,11 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
         f64 fx = -pmass * (f64) Fx, fy = -pmass * (f64) Fy, fz = -pmass * (f64) Fz;
         f64 tdu = pmass * (f64) U;
         u32 i     = rs.row_local[t];
+        if (ext.x) {
+            fx = fx + ext.x[i];
+            fy = fy + ext.y[i];
+            fz = fz + ext.z[i];
+        }
         size_t iv = (size_t) i * lf.vs;
         f64 ox = lf.ax[iv], oy = lf.ay[iv], oz = lf.az[iv], odu = lf.du[i];
         lf.ax[iv] = fx;
@@ -410,7 +415,7 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
 
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                               f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,
-                              f64 C_force, const LocalFields &lf) {
+                              f64 C_force, const LocalFields &lf, const ExtAccel &ext) {
     u32 N         = c.n_obj;
     MixedSpace ms = mixed_space(c, N);
     {
@@ -422,7 +427,7 @@ cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, 
     MixedParams p = mixed_params(pmass, alpha_u, alpha_AV, beta_AV);
     ProfScope ps(c, kProfDerivs, rs.n);
     { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, hs.h, hdt, C_cour,
-                                                                 C_force, lf,
+                                                                 C_force, lf, ext,
                                                                  c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     return cudaGetLastError();
 }

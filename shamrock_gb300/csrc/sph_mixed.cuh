@@ -30,7 +30,7 @@ cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h
 cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                               f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,
-                              f64 C_force, const LocalFields &lf);
+                              f64 C_force, const LocalFields &lf, const ExtAccel &ext);
 cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                                 f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
                                 f64 *du, f64 *vsig);

@@ -43,6 +43,9 @@ class SolverConfig:
         self.h_iter_per_subcycles = 50
         self.h_max_subcycles_count = 100
         self.precision = "fp64"
+        self.ext_forces = []
+        # G without a unit system is the SI value, as the reference's get_constant_G
+        self.constant_G = 6.6743e-11
 
     # -- setters named as the reference's python bindings
     def set_artif_viscosity_Constant(self, alpha_u, alpha_AV, beta_AV):
@@ -63,6 +66,22 @@ class SolverConfig:
 
     def set_eos_adiabatic(self, gamma):
         self.eos = dict(type="adiabatic", gamma=float(gamma))
+
+    def set_eos_locally_isothermalLP07(self, cs0, q, r0):
+        """c_s^2 = cs0^2 (R^2 / r0^2)^(-q), P = c_s^2 rho (pySPHModel.cpp:111-113)."""
+        self.eos = dict(type="locally_isothermal_lp07", cs0=float(cs0), q=float(q), r0=float(r0))
+
+    def add_ext_force_point_mass(self, central_mass, Racc):
+        """Central point mass at the origin (SolverConfig::add_ext_force_point_mass).
+        Accretion of particles inside Racc is not on the GB300 path: Racc must be 0."""
+        if Racc != 0:
+            raise ValueError("point-mass accretion is not on the GB300 path: use Racc=0")
+        self.ext_forces.append(dict(type="point_mass", central_mass=float(central_mass)))
+
+    def set_constant_G(self, G):
+        """Gravitational constant in code units (GB300 extension; the reference derives it
+        from the unit system, SI without one)."""
+        self.constant_G = float(G)
 
     def set_particle_mass(self, pmass):
         self.gpart_mass = float(pmass)
@@ -332,15 +351,27 @@ class Model:
 
     def _config_struct(self):
         c = self.cfg
-        if c.eos is None or c.eos["type"] != "adiabatic":
-            raise RuntimeError("set_eos_adiabatic must be called: only the adiabatic EOS is on "
-                               "the GB300 path")
+        if c.eos is None:
+            raise RuntimeError("an equation of state must be set (set_eos_adiabatic or "
+                               "set_eos_locally_isothermalLP07)")
+        if len(c.ext_forces) > 1:
+            raise RuntimeError("one external force (a point mass) at most on the GB300 path")
         if c.gpart_mass == 0:
             raise RuntimeError(f"invalid gpart_mass {c.gpart_mass}, this configuration can not "
                                "converge.\nPlease set it using either model.set_particle_mass(pmass)"
                                " or cfg.set_particle_mass(pmass)")
         s = L.Config()
-        s.gamma = c.eos["gamma"]
+        if c.eos["type"] == "adiabatic":
+            s.gamma = c.eos["gamma"]
+            s.eos_kind = 0
+        else:
+            s.gamma = 1.0
+            s.eos_kind = 1
+            s.cs0, s.eos_q, s.eos_r0 = c.eos["cs0"], c.eos["q"], c.eos["r0"]
+        if c.ext_forces:
+            s.ext_kind = 1
+            s.central_mass = c.ext_forces[0]["central_mass"]
+            s.constant_G = c.constant_G
         s.pmass = c.gpart_mass
         s.alpha_u, s.alpha_AV, s.beta_AV = c.av["alpha_u"], c.av["alpha_AV"], c.av["beta_AV"]
         s.cfl_cour, s.cfl_force = c.cfl_cour, c.cfl_force

@@ -152,3 +152,54 @@ def sound_wave(n_side=64, amp=1e-4, gamma=1.0001, cs=1.0, travelling=True, noise
         u = u * (1.0 + noise * rng.standard_normal(N))
     return dict(pos=pos, vel=vel, h=h, u=u, pmass=pmass, gamma=gamma,
                 box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0), periodic=True)
+
+def keplerian_disc(N, seed=12345, r_in=0.1, r_out=1.0, HoR=0.05, q=0.25, M=1.0, G=1.0,
+                   disc_mass=1e-3, jitter=0.1):
+    """Gas disc around a central point mass M at the origin: cylindrical radius r in
+    [r_in, r_out] with surface density Sigma ~ 1/r, locally isothermal sound speed
+    c_s = cs0 r^-q (r in units of r0 = 1) with cs0 = HoR so that H/R = HoR at r = 1,
+    vertical Gaussian of height H = c_s / Omega_K, Keplerian azimuthal velocity.
+
+    Sampling: a jittered lattice in (u_r, u_phi, u_z) in [0, 1]^3 mapped by the inverse
+    cumulative distributions (r uniform for Sigma ~ 1/r, phi uniform, z = H Phi^-1(u_z)),
+    with lattice counts that make the spacing nearly isotropic at mid radius, so no pair
+    starts much closer than the local spacing (see clustered_box)."""
+    from scipy.special import ndtri
+
+    rng = np.random.default_rng(seed)
+    cs0 = HoR
+    rm = 0.5 * (r_in + r_out)
+    Hm = cs0 * rm ** (1.5 - q)
+    dr_span, dphi_span, dz_span = r_out - r_in, 2 * np.pi * rm, 5.0 * Hm
+    # n_r : n_phi : n_z in proportion to the spans, product >= N
+    scale = (N / (dr_span * dphi_span * dz_span)) ** (1.0 / 3.0)
+    n1 = max(2, int(np.ceil(dr_span * scale)))
+    n2 = max(4, int(np.ceil(dphi_span * scale)))
+    n3 = max(2, int(np.ceil(dz_span * scale)))
+    while n1 * n2 * n3 < N:
+        n3 += 1
+    g1, g2, g3 = ((np.arange(k) + 0.5) / k for k in (n1, n2, n3))
+    a, b, c = np.meshgrid(g1, g2, g3, indexing="ij")
+    u = np.stack([a.ravel(), b.ravel(), c.ravel()], 1)
+    u += (jitter / np.array([n1, n2, n3])) * rng.standard_normal(u.shape)
+    u = u[rng.permutation(len(u))[:N]]
+    u[:, 0] = np.clip(u[:, 0], 0.0, 1.0)
+    u[:, 1] = np.mod(u[:, 1], 1.0)
+    u[:, 2] = np.clip(u[:, 2], 1e-4, 1.0 - 1e-4)
+    r = r_in + u[:, 0] * dr_span
+    phi = 2 * np.pi * u[:, 1]
+    cs_r = cs0 * r ** (-q)
+    H = cs_r / np.sqrt(G * M / r**3)
+    z = H * ndtri(u[:, 2])
+    pos = np.stack([r * np.cos(phi), r * np.sin(phi), z], 1)
+    vk = np.sqrt(G * M / r)
+    vel = np.stack([-vk * np.sin(phi), vk * np.cos(phi), np.zeros(N)], 1)
+    pmass = disc_mass / N
+    sigma = disc_mass / (2 * np.pi * dr_span * r)
+    rho = sigma * np.exp(-0.5 * (z / H) ** 2) / (np.sqrt(2 * np.pi) * H)
+    h = HFACT_M4 * (pmass / rho) ** (1.0 / 3.0)
+    Rsph = np.linalg.norm(pos, axis=1)
+    u_int = 1.5 * (cs0 * Rsph ** (-q)) ** 2
+    return dict(pos=pos, vel=vel, h=h, u=u_int, pmass=pmass, gamma=5.0 / 3.0, cs0=cs0, q=q,
+                r0=1.0, M=M, G=G, periodic=False,
+                box_min=tuple(pos.min(0) - 1e-3), box_max=tuple(pos.max(0) + 1e-3))

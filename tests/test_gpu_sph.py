@@ -194,3 +194,26 @@ def test_kdk_correct_and_cfl_vs_oracle(gctx):
     om, odtp = O.cfl(h, vsig, a_new, 0.3, 0.25)
     assert m == om
     assert np.array_equal(dtp.cpu().numpy(), odtp)
+
+
+def test_eos_locally_isothermal_vs_oracle(gctx):
+    import ctypes as C
+
+    from shamrock_gb300 import _lib as L
+    from shamrock_gb300 import modules as M
+
+    rng = np.random.default_rng(23)
+    n = 4000
+    pos = rng.normal(0, 0.5, (n, 3))
+    h = rng.uniform(0.01, 0.05, n)
+    x = M.soa(pos)
+    hh = torch.as_tensor(h, device="cuda")
+    P, cs = torch.empty_like(hh), torch.empty_like(hh)
+    gctx.call("gbsph_eos_locally_isothermal", L.Vec3(x[0].data_ptr(), x[1].data_ptr(),
+                                                       x[2].data_ptr(), 1, 0),
+              C.c_void_p(hh.data_ptr()), n, 1e-3 / n, 0.05, 1.0, 0.25, C.c_void_p(P.data_ptr()),
+              C.c_void_p(cs.data_ptr()), None)
+    oP, ocs = O.eos_locally_isothermal(pos, h, 1e-3 / n, 0.05, 1.0, 0.25)
+    # pow differs from the C library's in the last bits
+    assert np.allclose(P.cpu().numpy(), oP, rtol=1e-15, atol=0)
+    assert np.allclose(cs.cpu().numpy(), ocs, rtol=1e-15, atol=0)

@@ -155,3 +155,72 @@ def test_mixed_step_error(n_cells, jitter):
     assert _norm_err(g32["axyz"], g64["axyz"]) <= tol
     assert _norm_err(g32["duint"], g64["duint"]) <= tol
     assert _norm_err(g32["omega"], g64["omega"]) <= tol
+
+
+def _disc_pair(s, precision="fp64", alpha_AV=0.5):
+    import shamrock_gb300 as sg
+
+    ctx = sg.Context()
+    m = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
+    cfg = m.gen_default_config()
+    cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0)
+    cfg.set_boundary_free()
+    cfg.set_eos_locally_isothermalLP07(cs0=s["cs0"], q=s["q"], r0=s["r0"])
+    cfg.add_ext_force_point_mass(s["M"], 0.0)
+    cfg.set_constant_G(s["G"])
+    cfg.set_particle_mass(s["pmass"])
+    cfg.set_precision(precision)
+    m.set_solver_config(cfg)
+    m.resize_simulation_box(s["box_min"], s["box_max"])
+    m.set_particles(s["pos"], s["vel"], s["h"], s["u"])
+    m.set_cfl_cour(0.3)
+    m.set_cfl_force(0.3)
+    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_AV,
+                     beta_AV=2.0, cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0,
+                     htol_up_coarse=1.1, htol_up_fine=1.1, epsilon_h=1e-6,
+                     h_iter_per_subcycles=50, h_max_subcycles=100, tree_reduction_level=3,
+                     periodic=0, eos_kind=1, ext_kind=1, cs0=s["cs0"], eos_r0=s["r0"],
+                     eos_q=s["q"], central_mass=s["M"], constant_G=s["G"])
+    oc.bmin[:] = list(s["box_min"])
+    oc.bmax[:] = list(s["box_max"])
+    return m, O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
+
+
+def test_disc_locally_isothermal_point_mass_fp64_vs_oracle():
+    """Keplerian disc with the locally isothermal (LP07) EOS and the central point mass:
+    the FP64 step against the oracle.  c_s^2 goes through pow, whose last bit differs
+    between CUDA and the C library, so fields agree to round-off (1e-12) rather than bit
+    for bit; the step bookkeeping (leaves, cache, sub-cycles, iterations) is identical."""
+    from shamrock_gb300 import setups
+
+    s = setups.keplerian_disc(6000, seed=5)
+    model, sim = _disc_pair(s)
+    for k in range(3):
+        lg = model.evolve_once()
+        lo = sim.evolve_once()
+        for key in ("n_ghost", "leaf_count", "cache_size", "h_subcycles", "h_iterations",
+                    "corrector_iters"):
+            assert lg[key] == lo[key], (k, key, lg[key], lo[key])
+        assert lg["next_dt"] == pytest.approx(lo["next_dt"], rel=1e-12)
+        g, o = model.collect_data(), sim.get()
+        for f in ("xyz", "vxyz", "axyz", "hpart", "uint", "duint", "omega"):
+            scale = np.abs(o[f]).max()
+            assert np.abs(g[f] - o[f]).max() <= 1e-12 * scale, (k, f)
+
+
+def test_disc_mixed_vs_fp64_one_step():
+    """The same disc, one FP32-mixed step against one FP64 step from the same state:
+    h (density) per particle and |a|, du/dt normalised by their largest magnitude
+    within 1e-5."""
+    from shamrock_gb300 import setups
+
+    s = setups.keplerian_disc(20000, seed=6)
+    m64, _ = _disc_pair(s, "fp64")
+    m32, _ = _disc_pair(s, "mixed")
+    m64.evolve_once()
+    m32.evolve_once()
+    a, b = m32.collect_data(), m64.collect_data()
+    assert np.abs(a["hpart"] / b["hpart"] - 1).max() < 1e-5
+    for f in ("axyz", "duint"):
+        d = np.abs(a[f] - b[f]).max()
+        assert d <= 1e-5 * np.abs(b[f]).max(), (f, d / np.abs(b[f]).max())
