@@ -79,14 +79,21 @@ struct Src64 {
         f64 x, y, z, vx, vy, vz, u, h, om, lx, ly, lz, mu;
     };
     struct Nb {
-        f64 dx, dy, dz, dvx, dvy, dvz, u, h, om, lx, ly, lz, mu;
+        f64 dx, dy, dz, dvx, dvy, dvz, u, h, om, lx, ly, lz, mu, rsq;
     };
     __device__ Row row(u32 c) const {
         return Row{x[c], y[c], z[c], vx[c], vy[c], vz[c], u[c], h[c], om[c], lx[c], ly[c], lz[c], mu[c]};
     }
     __device__ Nb nb(u32 b, const Row &r) const {
-        return Nb{r.x - x[b], r.y - y[b], r.z - z[b], r.vx - vx[b], r.vy - vy[b], r.vz - vz[b],
-                  u[b],       h[b],       om[b],      lx[b],        ly[b],        lz[b],  mu[b]};
+        const f64 xb = x[b], yb = y[b], zb = z[b];
+        return Nb{r.x - xb, r.y - yb, r.z - zb, r.vx - vx[b], r.vy - vy[b], r.vz - vz[b],
+                  u[b],     h[b],     om[b],    lx[b],        ly[b],        lz[b],
+                  mu[b],    xb * xb + yb * yb + zb * zb};
+    }
+    __device__ void apos(const Row &r, f64 &ax, f64 &ay, f64 &az) const {
+        ax = r.x;
+        ay = r.y;
+        az = r.z;
     }
     __device__ void pos(u32 c, f64 &px, f64 &py, f64 &pz, f64 &ph) const {
         px = x[c];
@@ -118,7 +125,7 @@ struct Src32 {
         float4 l;
     };
     struct Nb {
-        float dx, dy, dz, dvx, dvy, dvz, u, h, om, lx, ly, lz, mu;
+        float dx, dy, dz, dvx, dvy, dvz, u, h, om, lx, ly, lz, mu, rsq;
     };
     __device__ Row row(u32 c) const {
         return Row{ldg256(&P[2 * (size_t) c]), ldg256(&V[2 * (size_t) c]), __ldg(&Lr[c])};
@@ -126,10 +133,16 @@ struct Src32 {
     __device__ Nb nb(u32 b, const Row &r) const {
         const F8 p = ldg256(&P[2 * (size_t) b]), v = ldg256(&V[2 * (size_t) b]);
         const float4 l = __ldg(&Lr[b]);
+        const float xb = p.a.x + p.b.x, yb = p.a.y + p.b.y, zb = p.a.z + p.b.z;
         return Nb{(r.p.a.x - p.a.x) + (r.p.b.x - p.b.x), (r.p.a.y - p.a.y) + (r.p.b.y - p.b.y),
                   (r.p.a.z - p.a.z) + (r.p.b.z - p.b.z), (r.v.a.x - v.a.x) + (r.v.b.x - v.b.x),
                   (r.v.a.y - v.a.y) + (r.v.b.y - v.b.y), (r.v.a.z - v.a.z) + (r.v.b.z - v.b.z),
-                  v.a.w, p.a.w, p.b.w, l.x, l.y, l.z, v.b.w};
+                  v.a.w, p.a.w, p.b.w, l.x, l.y, l.z, v.b.w, xb * xb + yb * yb + zb * zb};
+    }
+    __device__ void apos(const Row &r, float &ax, float &ay, float &az) const {
+        ax = r.p.a.x + r.p.b.x;
+        ay = r.p.a.y + r.p.b.y;
+        az = r.p.a.z + r.p.b.z;
     }
     __device__ void pos(u32 c, F8 &pc, float &ph) const {
         pc = ldg256(&P[2 * (size_t) c]);
@@ -226,7 +239,7 @@ __global__ void k_adj_stage32m(u32 N, u32 n, const u32 *__restrict__ sort_index,
 }
 
 // -------------------------------------------------------------- reverse of derivs
-template<class Src>
+template<class Src, bool LP07>
 __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjParams p,
                                                     AdjLocal L, f64 *g_alpha) {
     using T    = typename Src::T;
@@ -241,7 +254,13 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
         const auto self = src.nb(c, rc); // the row's own scalars (differences are zero)
         const T uc = self.u, hc = self.h, omc = self.om;
         const T lxc = self.lx, lyc = self.ly, lzc = self.lz, muc = self.mu;
-        const T rhoc = rho_of_h(m, hc), Pc = gm1 * rhoc * uc, csc = sqrt(gam * gm1 * uc);
+        constexpr bool lp07 = LP07;
+        const T cs0sq = T(p.cs0 * p.cs0), ir0sq = T(1 / (p.r0 * p.r0)), mq = T(-p.q);
+        const T rhoc = rho_of_h(m, hc);
+        // adiabatic: P = (gamma - 1) rho u; LP07: c_s^2 = cs0^2 (R^2 / r0^2)^(-q), P = c_s^2 rho
+        const T csqc = lp07 ? cs0sq * pow(self.rsq * ir0sq, mq) : gam * gm1 * uc;
+        const T Pc   = lp07 ? csqc * rhoc : gm1 * rhoc * uc;
+        const T csc  = sqrt(csqc);
         const T subc = rhoc * rhoc * omc;
         const T kc = (subc != T(0) && subc == subc) ? T(1) / subc : T(0), jc = T(1) / (rhoc * omc);
         const T ihc = T(1) / hc, ihc4 = ihc * ihc * ihc * ihc;
@@ -259,7 +278,10 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             const T r = sqrt(r2), ir = T(1) / r;
             const T ex = dx * ir, ey = dy * ir, ez = dz * ir;
             const T ub = nb.u, omb = nb.om;
-            const T rhob = rho_of_h(m, hb), Pb = gm1 * rhob * ub, csb = sqrt(gam * gm1 * ub);
+            const T rhob = rho_of_h(m, hb);
+            const T csqb = lp07 ? cs0sq * pow(nb.rsq * ir0sq, mq) : gam * gm1 * ub;
+            const T Pb   = lp07 ? csqb * rhob : gm1 * rhob * ub;
+            const T csb  = sqrt(csqb);
             const T subb = rhob * rhob * omb;
             const T kb = (subb != T(0) && subb == subb) ? T(1) / subb : T(0), jb = T(1) / (rhob * omb);
             const T ihb = T(1) / hb;
@@ -326,20 +348,36 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             ga += -m * lce * (kc * Fc * dqca + kb * Fb * dqba) + muc * m * w * kc * Fc * dqca;
         }
         const f64 rhoc_ = rhoc, kc_ = kc, jc_ = jc, omc_ = omc, hc_ = hc;
-        const f64 gu = (f64) sP * (p.gamma - 1) * rhoc_
-                       + (csc > T(0) ? (f64) scs * p.gamma * (p.gamma - 1) / (2 * (f64) csc) : 0)
-                       + (f64) su;
-        const f64 grho = (f64) sP * (p.gamma - 1) * (f64) uc + (f64) srho
-                         + (f64) sk * (-2 * kc_ / rhoc_) + (f64) sj * (-jc_ / rhoc_);
+        f64 gu, grho, gpx = 0, gpy = 0, gpz = 0;
+        if constexpr (lp07) {
+            // P, c_s depend on the position and rho, not on u
+            gu   = (f64) su;
+            grho = (f64) sP * (f64) csqc + (f64) srho + (f64) sk * (-2 * kc_ / rhoc_)
+                   + (f64) sj * (-jc_ / rhoc_);
+            // d c_s^2 / d x = -2 q c_s^2 x / R^2
+            T ax, ay, az;
+            src.apos(rc, ax, ay, az);
+            const f64 dcs2 = -2 * p.q * (f64) csqc / (f64) self.rsq;
+            const f64 coef = ((f64) sP * rhoc_ + (csc > T(0) ? (f64) scs / (2 * (f64) csc) : 0)) * dcs2;
+            gpx = coef * (f64) ax;
+            gpy = coef * (f64) ay;
+            gpz = coef * (f64) az;
+        } else {
+            gu = (f64) sP * (p.gamma - 1) * rhoc_
+                 + (csc > T(0) ? (f64) scs * p.gamma * (p.gamma - 1) / (2 * (f64) csc) : 0)
+                 + (f64) su;
+            grho = (f64) sP * (p.gamma - 1) * (f64) uc + (f64) srho
+                   + (f64) sk * (-2 * kc_ / rhoc_) + (f64) sj * (-jc_ / rhoc_);
+        }
         const f64 gh  = grho * (-3 * rhoc_ / hc_) + (f64) shF;
         const f64 gom = (f64) sk * (-kc_ / omc_) + (f64) sj * (-jc_ / omc_);
         L.lv[0][i] += gvx;
         L.lv[1][i] += gvy;
         L.lv[2][i] += gvz;
         L.lu[i] += gu;
-        L.gx[0][i] += gxr;
-        L.gx[1][i] += gyr;
-        L.gx[2][i] += gzr;
+        L.gx[0][i] += (f64) gxr + gpx;
+        L.gx[1][i] += (f64) gyr + gpy;
+        L.gx[2][i] += (f64) gzr + gpz;
         L.gh[i] += gh;
         L.gom[i] += gom;
         galpha = ga;
@@ -430,6 +468,23 @@ __global__ void __launch_bounds__(256) k_adj_omega_b(RowSpace rs, Src src, f64 p
     L.gx[0][i] += gx;
     L.gx[1][i] += gy;
     L.gx[2][i] += gz;
+}
+
+// -------------------------------------------------------------- external point mass
+// a_ext = mGM r / |r|^3 at the local positions x' of the step: gx += (d a_ext / d x)^T lam
+// = mGM (lam / r^3 - 3 r (r . lam) / r^5) for the cotangent lam of the corrector
+// evaluation being reversed.
+__global__ void k_adj_ext(u32 n, const f64 *__restrict__ xl, const f64 *__restrict__ yl,
+                          const f64 *__restrict__ zl, f64 mGM, AdjLocal L) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f64 x = xl[i], y = yl[i], z = zl[i];
+    const f64 r2 = x * x + y * y + z * z, r = sqrt(r2), ir3 = 1 / (r2 * r), ir5 = ir3 / r2;
+    const f64 lx = L.lam[0][i], ly = L.lam[1][i], lz = L.lam[2][i];
+    const f64 rl = x * lx + y * ly + z * lz;
+    L.gx[0][i] += mGM * (lx * ir3 - 3 * x * rl * ir5);
+    L.gx[1][i] += mGM * (ly * ir3 - 3 * y * rl * ir5);
+    L.gx[2][i] += mGM * (lz * ir3 - 3 * z * rl * ir5);
 }
 
 // -------------------------------------------------------------- linear steps
@@ -532,17 +587,24 @@ cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_loc
     for (u32 k = K; k >= 1; k--) {
         { k_adj_lin<<<gb, 256, 0, s>>>(n, 0, hdt, L); GBSPH_COUNTED; }
         const f64 *sv = snap + (size_t) (k - 1) * 4 * n_;
+        if (p.ext_x) { k_adj_ext<<<gb, 256, 0, s>>>(n, p.ext_x, p.ext_y, p.ext_z, p.mGM, L); GBSPH_COUNTED; }
         ProfScope ps(c, kProfAdjDerivs, n);
         if (fp32) {
             { k_adj_stage32<<<gN, 256, 0, s>>>(N, n, si, gs, rs.x, rs.y, rs.z, sv, sv + n_,
                                              sv + 2 * n_, sv + 3 * n_, h_local, omega_local,
                                              L.lam[0], L.lam[1], L.lam[2], L.mu, P32, V32, L32); GBSPH_COUNTED; }
-            { k_adj_derivs<Src32><<<div_up(n, 128), 128, 0, s>>>(rs, s32, p, L, g_alpha); GBSPH_COUNTED; }
+            if (p.eos_kind == 1)
+                { k_adj_derivs<Src32, true><<<div_up(n, 128), 128, 0, s>>>(rs, s32, p, L, g_alpha); GBSPH_COUNTED; }
+            else
+                { k_adj_derivs<Src32, false><<<div_up(n, 128), 128, 0, s>>>(rs, s32, p, L, g_alpha); GBSPH_COUNTED; }
         } else {
             { k_adj_gather<<<gN, 256, 0, s>>>(N, n, si, gs, sv, sv + n_, sv + 2 * n_, sv + 3 * n_,
                                             h_local, omega_local, L.lam[0], L.lam[1], L.lam[2],
                                             L.mu, R); GBSPH_COUNTED; }
-            { k_adj_derivs<Src64><<<div_up(n, 128), 128, 0, s>>>(rs, s64, p, L, g_alpha); GBSPH_COUNTED; }
+            if (p.eos_kind == 1)
+                { k_adj_derivs<Src64, true><<<div_up(n, 128), 128, 0, s>>>(rs, s64, p, L, g_alpha); GBSPH_COUNTED; }
+            else
+                { k_adj_derivs<Src64, false><<<div_up(n, 128), 128, 0, s>>>(rs, s64, p, L, g_alpha); GBSPH_COUNTED; }
         }
         { k_adj_lin<<<gb, 256, 0, s>>>(n, 1, hdt, L); GBSPH_COUNTED; }
     }

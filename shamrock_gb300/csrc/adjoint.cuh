@@ -17,6 +17,13 @@ constexpr u32 kTapeMaxIters = 16;
 
 struct AdjParams {
     f64 pmass, gamma, alpha_u, alpha_AV, beta_AV, dt;
+    // equation of state: 0 adiabatic, 1 locally isothermal LP07 (c_s^2 = cs0^2 (R^2/r0^2)^-q)
+    u32 eos_kind;
+    f64 cs0, r0, q;
+    // central point mass (mGM = -G M; ext_x null when absent) and the local positions
+    // after the step it was evaluated at
+    f64 mGM;
+    const f64 *ext_x, *ext_y, *ext_z;
 };
 
 // Cotangents of one particle state (SoA), updated in place by adjoint_backward: on

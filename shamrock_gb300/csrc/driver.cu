@@ -794,8 +794,12 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     REQUIRE_ARG(cot->gx.stride == cot->gv.stride && cot->gx.stride == cot->ga.stride,
                 "gx, gv and ga must share one element stride");
     REQUIRE_ARG(dt >= 0, "dt must be the forward step's dt");
-    REQUIRE_ARG(cfg->eos_kind == GBSPH_EOS_ADIABATIC && cfg->ext_kind == GBSPH_EXT_NONE,
-                "the adjoint covers the adiabatic EOS without external forces");
+    REQUIRE_ARG(cfg->eos_kind == GBSPH_EOS_ADIABATIC || cfg->eos_kind == GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07,
+                "unknown equation of state");
+    REQUIRE_ARG((cfg->eos_kind == GBSPH_EOS_ADIABATIC && cfg->ext_kind == GBSPH_EXT_NONE) ||
+                    !cfg->periodic,
+                "the adjoint of the locally isothermal EOS or the point mass needs free "
+                "boundaries (a periodic image's pressure depends on its shifted position)");
     cudaStream_t s = c.stream;
     const u32 n    = start->n;
     // recompute the step on a working copy of the start state
@@ -823,7 +827,14 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     RowSpace rs{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
                 c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
                 c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
-    AdjParams ap{cfg->pmass, cfg->gamma, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV, dt};
+    AdjParams ap{cfg->pmass, cfg->gamma, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV, dt,
+                 cfg->eos_kind, cfg->cs0, cfg->eos_r0 > 0 ? cfg->eos_r0 : 1.0, cfg->eos_q,
+                 -cfg->central_mass * cfg->constant_G, nullptr, nullptr, nullptr};
+    if (cfg->ext_kind == GBSPH_EXT_POINT_MASS) {
+        ap.ext_x = w.xyz.x;
+        ap.ext_y = w.xyz.y;
+        ap.ext_z = w.xyz.z;
+    }
     CotState cs;
     cs.x[0] = cot->gx.x; cs.x[1] = cot->gx.y; cs.x[2] = cot->gx.z;
     cs.v[0] = cot->gv.x; cs.v[1] = cot->gv.y; cs.v[2] = cot->gv.z;
