@@ -43,10 +43,12 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--workload", default="sedov",
-                   choices=["sedov", "sedov_plain", "clustered", "soundwave"],
+                   choices=["sedov", "sedov_plain", "clustered", "soundwave", "disc"],
                    help="sedov: jittered Sedov-Taylor (default, 4*cells^3); sedov_plain: the "
                         "same without jitter; clustered: 8,388,608 particles, half uniform, "
-                        "half in a Gaussian clump; soundwave: 64^3 travelling sound wave")
+                        "half in a Gaussian clump; soundwave: 64^3 travelling sound wave; "
+                        "disc: 4,194,304-particle Keplerian disc (locally isothermal EOS, "
+                        "central point mass, free boundary)")
     p.add_argument("--cells", type=int, default=64, help="FCC cells per axis (4*cells^3 particles)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -68,6 +70,12 @@ def workload(cells, kind="sedov"):
                 "v ~ N(0, 0.1^2), u ~ U[0.5, 1.5], gamma 5/3, M4, constant AV a=1 b=2, "
                 "CFL 0.3, periodic, tree rebuilt every step)")
         return s, name, 1.0
+    if kind == "disc":
+        s = setups.keplerian_disc(4194304, seed=12345)
+        name = ("keplerian_disc_4194304 (point mass M=1 G=1, r in [0.1, 1], Sigma ~ 1/r, H/R 0.05 "
+                "at r=1, locally isothermal LP07 c_s ~ r^-0.25, constant AV a=0.5 b=2, CFL 0.3, "
+                "free boundary, tree rebuilt every step)")
+        return s, name, 0.5
     if kind == "soundwave":
         s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
         name = ("sound_wave_cubic_64^3 (N=262144, amp 1e-4, gamma 1.0001, constant AV "
@@ -87,8 +95,16 @@ def make_model(s, precision, device=0, alpha_AV=1.0):
     m = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
     cfg = m.gen_default_config()
     cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0)
-    cfg.set_boundary_periodic()
-    cfg.set_eos_adiabatic(s["gamma"])
+    if s.get("periodic", True):
+        cfg.set_boundary_periodic()
+    else:
+        cfg.set_boundary_free()
+    if "cs0" in s:
+        cfg.set_eos_locally_isothermalLP07(cs0=s["cs0"], q=s["q"], r0=s["r0"])
+        cfg.add_ext_force_point_mass(s["M"], 0.0)
+        cfg.set_constant_G(s["G"])
+    else:
+        cfg.set_eos_adiabatic(s["gamma"])
     cfg.set_particle_mass(s["pmass"])
     cfg.set_precision(precision)
     m.set_solver_config(cfg)
@@ -261,6 +277,23 @@ def reference_rank_runs(world, rank):
     return world <= 1 or rank == 0
 
 
+def oracle_config(O, s, alpha_AV):
+    """The oracle's configuration of workload `s` (same solver settings as make_model)."""
+    disc = "cs0" in s
+    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0,
+                     cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
+                     htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
+                     h_max_subcycles=100, tree_reduction_level=3,
+                     periodic=1 if s.get("periodic", True) else 0)
+    if disc:
+        oc.eos_kind, oc.ext_kind = 1, 1
+        oc.cs0, oc.eos_r0, oc.eos_q = s["cs0"], s["r0"], s["q"]
+        oc.central_mass, oc.constant_G = s["M"], s["G"]
+    oc.bmin[:] = list(s["box_min"])
+    oc.bmax[:] = list(s["box_max"])
+    return oc
+
+
 def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     """FP64 oracle (OpenMP) on the same workload, bounded to about `seconds`."""
     from oracle import oracle as O
@@ -268,12 +301,7 @@ def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     if threads:
         O.set_threads(threads)
     cores = O.get_threads()
-    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0,
-                     cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
-                     htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
-                     h_max_subcycles=100, tree_reduction_level=3, periodic=1)
-    oc.bmin[:] = list(s["box_min"])
-    oc.bmax[:] = list(s["box_max"])
+    oc = oracle_config(O, s, alpha_AV)
     sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
     sim.evolve_once()  # dt = 0 step (h convergence, first CFL), untimed
     n = len(s["h"])
@@ -300,12 +328,7 @@ def run_reference(args):
 
     O.set_threads(os.cpu_count())
     cores = O.get_threads()
-    oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_av, beta_AV=2.0,
-                     cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
-                     htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
-                     h_max_subcycles=100, tree_reduction_level=3, periodic=1)
-    oc.bmin[:] = list(s["box_min"])
-    oc.bmax[:] = list(s["box_max"])
+    oc = oracle_config(O, s, alpha_av)
     sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
     n = len(s["h"])
     for _ in range(max(1, min(args.warmup, 2))):
@@ -471,7 +494,11 @@ def run_gb300(args):
         if args.precision == "mixed":
             line["mixed_over_fp64"] = value / v64
     if world == 1 and not args.no_adjoint:
-        line["adjoint"] = adjoint_bench(precision=args.precision, device=local)
+        if args.workload == "disc":
+            line["adjoint"] = adjoint_bench(steps=50, ck=5, precision=args.precision, device=local,
+                                            workload="disc")
+        else:
+            line["adjoint"] = adjoint_bench(precision=args.precision, device=local)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, args.cpu_seconds, threads=os.cpu_count(),
                                             alpha_AV=alpha_av)
@@ -479,19 +506,26 @@ def run_gb300(args):
     return 0
 
 
-def adjoint_bench(steps=40, ck=5, precision="mixed", device=0):
-    """Adjoint / forward time of the differentiable sound-wave rollout: 2^18 particles
-    (simple cubic 64^3), density perturbation 1e-4 sin(2 pi x), gamma 1.0001, alpha_AV
-    0.1; loss = |v_final - v_target|^2 (seeded target) after `steps` steps; gradients
-    with respect to initial v, u and alpha_AV with a checkpoint every `ck` steps.  The
-    backward time includes the recomputation between checkpoints."""
+def adjoint_bench(steps=40, ck=5, precision="mixed", device=0, workload="soundwave"):
+    """Adjoint / forward time of a differentiable rollout of `steps` steps with a
+    checkpoint every `ck` steps; gradients with respect to initial v, u and alpha_AV.
+    soundwave: 2^18 particles (simple cubic 64^3), density perturbation 1e-4 sin(2 pi x),
+    gamma 1.0001, alpha_AV 0.1, loss = |v_final - v_target|^2 (seeded target).
+    disc: the 4,194,304-particle Keplerian disc (locally isothermal EOS, central point
+    mass, free boundary), alpha_AV 0.5, loss = total kinetic energy.  The backward time
+    includes the recomputation between checkpoints."""
     import numpy as np
     import torch
 
     from shamrock_gb300 import adjoint, setups
 
-    s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
-    m = make_model(s, precision, device, alpha_AV=0.1)
+    if workload == "disc":
+        s = setups.keplerian_disc(4194304, seed=12345)
+        alpha0 = 0.5
+    else:
+        s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
+        alpha0 = 0.1
+    m = make_model(s, precision, device, alpha_AV=alpha0)
     m.evolve_once()  # dt = 0: initial h, Omega, a, du
     d = m._to_device()
     n = d["hpart"].shape[0]
@@ -499,14 +533,21 @@ def adjoint_bench(steps=40, ck=5, precision="mixed", device=0):
     v_t = torch.as_tensor(1e-4 * rng.standard_normal((3, n)), device=d["vxyz"].device)
     v0 = d["vxyz"].clone().requires_grad_(True)
     u0 = d["uint"].clone().requires_grad_(True)
-    alpha = torch.tensor(0.1, dtype=torch.float64, requires_grad=True)
+    alpha = torch.tensor(alpha0, dtype=torch.float64, requires_grad=True)
+
+    def loss_of(v):
+        # disc: total kinetic energy; sound wave: distance to a seeded target field
+        if workload == "disc":
+            return 0.5 * s["pmass"] * (v * v).sum()
+        return ((v - v_t) ** 2).sum()
+
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     lib = m._lib()
     # untimed warm-up rollout + backward (lazy kernel loading, autograd worker thread)
     warm = adjoint._snapshot(m)
     t_w, dt_w, cm_w = m.time, m.dt, m.cfl_mult
     xw, vw, uw = adjoint.rollout(m, v0, u0, alpha, ck, ck)
-    ((vw - v_t) ** 2).sum().backward()
+    loss_of(vw).backward()
     v0.grad = u0.grad = alpha.grad = None
     adjoint._restore(m, warm)
     m.time, m.dt, m.cfl_mult = t_w, dt_w, cm_w
@@ -514,7 +555,7 @@ def adjoint_bench(steps=40, ck=5, precision="mixed", device=0):
     ev[0].record()
     x, v, u = adjoint.rollout(m, v0, u0, alpha, steps, ck)
     ev[1].record()
-    loss = ((v - v_t) ** 2).sum()
+    loss = loss_of(v)
     torch.cuda.synchronize()
     lib.profile(True)
     ev[2].record()
@@ -525,8 +566,11 @@ def adjoint_bench(steps=40, ck=5, precision="mixed", device=0):
     lib.profile(False)
     f_ms, b_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
     iters = [r[2] for r in adjoint.rollout.last_records]
-    return {"workload": "sound_wave_cubic_64^3 (N=%d, amp 1e-4, gamma 1.0001, "
-                        "alpha_AV 0.1, periodic)" % n,
+    wname = ("keplerian_disc_4194304 (LP07, point mass, alpha_AV 0.5, free boundary); loss = "
+             "total kinetic energy" if workload == "disc" else
+             "sound_wave_cubic_64^3 (N=%d, amp 1e-4, gamma 1.0001, alpha_AV 0.1, periodic); loss "
+             "= |v - v_target|^2" % n)
+    return {"workload": wname,
             "precision": precision, "steps": steps, "checkpoint_every": ck,
             "forward_ms": f_ms, "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
             "loss": float(loss.detach()),
