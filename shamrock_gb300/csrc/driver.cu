@@ -60,7 +60,7 @@ Ctx::~Ctx() {
                       &offsets, &reduc, &reduced, &lchild, &rchild, &lflag, &rflag, &endrange,
                       &parent, &boxes, &visit, &fboxes, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
                       &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
-                      &owner, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
+                      &owner, &leaf_thr, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
                       &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
@@ -704,8 +704,13 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         CU(cudaMemcpyAsync(p->omega, c.omega_local.p, 8 * (size_t) n, cudaMemcpyDeviceToDevice, s));
 
     // ---- corrector loop (Solver.cpp:2247-3171)
+    // FP64 rank-ordered hydro copies (the mixed path stages 32-byte records and keeps
+    // only h in FP64)
     DevBuf *rank_bufs[] = {&c.sh2, &c.su, &c.svx, &c.svy, &c.svz, &c.som, &c.sP, &c.scs};
-    for (DevBuf *b : rank_bufs) CU(b->ensure(8 * (size_t) N, s));
+    for (DevBuf *b : rank_bufs) {
+        CU(b->ensure(8 * (size_t) N, s));
+        if (mixed) break;
+    }
     if (tape) {
         CU(tape->snap->ensure(sizeof(f64) * 4 * (size_t) n * tape->forced_iters, s));
         tape->iters = 0;
@@ -720,7 +725,8 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             return fail(ctx, GBSPH_ERR_NOT_CONVERGED,
                         "the corrector has made over 50 loops, either their is a bug, either you "
                         "are using a dt that is too large");
-        CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
+        if (mixed) CU(gather_stage_mixed(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
+        else CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
         if (tape) {
             { k_snap_vu<<<div_up(n, 256), 256, 0, s>>>(
                 n, lf.vx, lf.vy, lf.vz, lf.vs, lf.u,
@@ -731,7 +737,7 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         f64 C_cour  = cfg->cfl_cour * ts->cfl_mult;
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
         if (mixed)
-            CU(derivs_step_mixed(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
+            CU(derivs_step_mixed(c, rs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
                                  dt / 2, C_cour, C_force, lf, ext));
         else
             CU(derivs_step64(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,

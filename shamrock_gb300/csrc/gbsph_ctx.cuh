@@ -118,6 +118,7 @@ struct Ctx {
     u64 slot_budget = 0;            // bytes of one-pass slots allowed (0: library default)
     DevBuf leaf_cnt, leaf_off, leaf_ent; // stage 1 (leaf ids)
     DevBuf owner;                        // per row: leaf index
+    DevBuf leaf_thr;                     // per leaf: FP32 bits of max thr over its owned rows
     DevBuf csr_cnt, csr_off, csr_ent;    // stage 2, per row, entries are ranks
     u32 n_local = 0;
     bool cache_valid = false;

@@ -146,11 +146,22 @@ __global__ void k_boxes_f32(const NodeBox *__restrict__ b, u32 T, NodeBoxF *__re
 
 __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *__restrict__ fb,
                                                     u32 *__restrict__ cnt, u32 *__restrict__ off,
-                                                    u32 *__restrict__ ent, u32 cap, Scalars *sc) {
+                                                    u32 *__restrict__ ent, u32 cap, Scalars *sc,
+                                                    const u32 *__restrict__ leaf_thr) {
     u32 l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= t.L) return;
-    LeafCrit crit(t, l);
     u32 c = 0, base = l * cap;
+    float thr_own = 0.f;
+    if (leaf_thr) {
+        const u32 tb = leaf_thr[l];
+        if (tb == 0) { // no row is owned by this leaf: stage 2 never reads its list
+            cnt[l] = 0;
+            off[l] = base;
+            return;
+        }
+        thr_own = __uint_as_float(tb);
+    }
+    LeafCrit crit(t, l);
     bool ok;
     if (fb) {
         F8 fa = ldg256(&fb[t.off() + l]), fr = ldg256(&fb[0]);
@@ -158,11 +169,14 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
         float M = fmaxf(fmaxf(fmaxf(fabsf(rlo.x), fabsf(rlo.y)), fmaxf(fabsf(rlo.z), fabsf(rhi.x))),
                         fmaxf(fabsf(rhi.y), fabsf(rhi.z)));
         float band_abs = 1e-6f * M;
+        float4 llo = alo, lhi = ahi; // box of the node last tested
         ok = dfs(
             t,
             [&](u32 node) {
                 F8 fn = ldg256(&fb[node]);
                 const float4 nlo = fn.a, nhi = fn.b;
+                llo = nlo;
+                lhi = nhi;
                 float sx = fmaxf(nlo.x - ahi.x, alo.x - nhi.x);
                 float sy = fmaxf(nlo.y - ahi.y, alo.y - nhi.y);
                 float sz = fmaxf(nlo.z - ahi.z, alo.z - nhi.z);
@@ -174,6 +188,21 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
                 return crit(node);
             },
             [&](u32 leaf) {
+                if (leaf_thr) {
+                    // Exact pruning for stage 2 (the cache stays the same): every row
+                    // owned by this leaf lies in its box, so a pair (a, b) with b in
+                    // `leaf` has r_ab at least the Euclidean gap D between the boxes.
+                    // With thr_own >= thr_a of every owned row and (r_leaf R)^2 >= thr_b,
+                    // D^2 > max of the two makes every pair test fail.  The FP32 gaps
+                    // are shrunk by the rounding band and the bound carries a 1e-5
+                    // margin, so the skip is certain.
+                    float gx = fmaxf(fmaxf(llo.x - ahi.x, alo.x - lhi.x) - band_abs, 0.f);
+                    float gy = fmaxf(fmaxf(llo.y - ahi.y, alo.y - lhi.y) - band_abs, 0.f);
+                    float gz = fmaxf(fmaxf(llo.z - ahi.z, alo.z - lhi.z) - band_abs, 0.f);
+                    float d2 = gx * gx + gy * gy + gz * gz;
+                    float tb = fmaxf(thr_own, llo.w * llo.w * 1.000001f);
+                    if (d2 > tb * 1.00001f) return;
+                }
                 if (c < cap) ent[base + c] = leaf;
                 c++;
             });
@@ -211,9 +240,12 @@ __global__ void k_rows(const u32 *__restrict__ sort_index, const u8 *__restrict_
 
 // ---- owner leaf: max leaf index whose box contains the point (inclusive bounds),
 // i.e. the last leaf the reference's left-first DFS reports (NeighbourCache.cpp:419-443)
+// leaf_thr (optional): per leaf, the FP32 bits (rounded up) of the largest pair-test
+// threshold thr_a = ((h_a htol)^2) R^2 over the rows it owns, 0 for a leaf owning none.
 __global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows,
                         const f64 *__restrict__ sx, const f64 *__restrict__ sy,
-                        const f64 *__restrict__ sz, u32 *__restrict__ owner, u32 *__restrict__ flags) {
+                        const f64 *__restrict__ sz, u32 *__restrict__ owner, u32 *__restrict__ flags,
+                        const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ leaf_thr) {
     u32 row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n_rows) return;
     u32 r    = row_rank[row];
@@ -244,6 +276,10 @@ __global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows
     if (found == kNone) {
         atomicOr(flags, kFlagOwnerMissing);
         found = 0;
+    } else if (leaf_thr) {
+        f64 rint_a = __dmul_rn(sh[r], h_tol);
+        f64 thr_a  = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
+        atomicMax(&leaf_thr[found], __float_as_uint(__double2float_ru(thr_a)));
     }
     owner[row] = found;
 }
@@ -432,12 +468,28 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         { k_boxes_f32<<<div_up(T, 256), 256, 0, s>>>(c.boxes.as<NodeBox>(), T, c.fboxes.as<NodeBoxF>()); GBSPH_COUNTED; }
         fb = c.fboxes.as<NodeBoxF>();
     }
+    // Owner leaves first.  With FP32 boxes it also records, per leaf, the largest
+    // threshold of the rows it owns, which lets stage 1 drop leaves that no owned row
+    // can pair with (and skip leaves that own no row); the cache is unchanged.
+    if ((e = c.owner.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
+    u32 *leaf_thr = nullptr;
+    if (fb) {
+        if ((e = c.leaf_thr.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(c.leaf_thr.p, 0, sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+        leaf_thr = c.leaf_thr.as<u32>();
+    }
+    if (n) {
+        ProfScope ps(c, kProfOwner, n);
+        { k_owner<<<div_up(n, 128), 128, 0, s>>>(t, c.row_rank.as<u32>(), n, c.sx.as<f64>(),
+                                               c.sy.as<f64>(), c.sz.as<f64>(), c.owner.as<u32>(),
+                                               &dsc->flags, c.sh.as<f64>(), h_tol, leaf_thr); GBSPH_COUNTED; }
+    }
     auto stage1 = [&]() -> cudaError_t {
         cudaError_t err = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * c.leaf_cap + 1), s);
         if (err != cudaSuccess) return err;
         ProfScope ps(c, kProfStage1, L);
         { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
-                                                    c.leaf_ent.as<u32>(), c.leaf_cap, dsc); GBSPH_COUNTED; }
+                                                    c.leaf_ent.as<u32>(), c.leaf_cap, dsc, leaf_thr); GBSPH_COUNTED; }
         return cudaGetLastError();
     };
     if (s1_one_pass) {
@@ -447,13 +499,6 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         const u32 ovf = kFlagLeafCap;
         if ((e = cudaMemcpyAsync(&dsc->flags, &ovf, sizeof(u32), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(&dsc->leaf_cnt_max, &c.leaf_cap, sizeof(u32), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
-    }
-    if ((e = c.owner.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
-    if (n) {
-        ProfScope ps(c, kProfOwner, n);
-        { k_owner<<<div_up(n, 128), 128, 0, s>>>(t, c.row_rank.as<u32>(), n, c.sx.as<f64>(),
-                                               c.sy.as<f64>(), c.sz.as<f64>(), c.owner.as<u32>(),
-                                               &dsc->flags); GBSPH_COUNTED; }
     }
     if ((e = sync_scalars(c)) != cudaSuccess) return e;
     if (c.h_scalars->flags & (kFlagStackOverflow | kFlagOwnerMissing)) {

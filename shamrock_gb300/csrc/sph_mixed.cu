@@ -114,6 +114,61 @@ __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__res
                             pack_bf16x2(lo32(vz), lo32(Pr)));
 }
 
+// EOS and hydro staging of the corrector loop in one pass (the FP64 path runs
+// k_gather_eos into FP64 rank-ordered copies instead): per merged rank r, the source
+// particle's fields (a local id, or a ghost's source), its pressure and sound speed,
+// written as whole 32-byte position and hydro records.  Pressure and c_s follow
+// ComputeEos.cpp (adiabatic: P = (gamma - 1) rho u, c_s = sqrt(gamma P / rho) =
+// sqrt(gamma (gamma - 1) u); locally isothermal LP07: c_s^2 = cs0^2 (R^2/r0^2)^-q at the
+// merged position, P = c_s^2 rho), and the FP64 h in rank order for the CFL step of the
+// derivatives kernel.  c_s is stored in FP32, so it and the LP07 power are
+// evaluated in FP32 (relative error ~2e-7, the size of the records' own rounding); rho,
+// P and 1/(rho^2 Omega) stay FP64 until they are split into the record.
+struct StageEos {
+    u32 kind;     // 0 adiabatic, 1 locally isothermal LP07
+    f64 gamma;
+    float gg;     // gamma (gamma - 1)
+    f64 inv_r0sq; // 1 / r0^2
+    float cs0sq, mq;
+};
+
+__global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
+                                     const u32 *__restrict__ ghost_src, LocalFields lf,
+                                     const f64 *__restrict__ omega, f64 pmass, StageEos eos,
+                                     const f64 *__restrict__ sx, const f64 *__restrict__ sy,
+                                     const f64 *__restrict__ sz, float4 *__restrict__ P,
+                                     float4 *__restrict__ H, f64 *__restrict__ h_rank) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    u32 id  = sort_index[r];
+    u32 src = id < n_local ? id : ghost_src[id - n_local];
+    size_t iv = (size_t) src * lf.vs;
+    f64 hh = lf.h[src], uu = lf.u[src], om = omega[src];
+    f64 vx = lf.vx[iv], vy = lf.vy[iv], vz = lf.vz[iv];
+    f64 x = sx[r], y = sy[r], z = sz[r];
+    h_rank[r] = hh;
+    f64 rho   = rho_h64(pmass, hh);
+    f64 Pr;
+    float cs;
+    if (eos.kind == 1) {
+        float ratio = __double2float_rn((x * x + y * y + z * z) * eos.inv_r0sq);
+        float cs_sq = eos.cs0sq * powf(ratio, eos.mq);
+        Pr          = (f64) cs_sq * rho;
+        cs          = sqrtf(cs_sq);
+    } else {
+        Pr = (eos.gamma - 1) * rho * uu;
+        cs = sqrtf(eos.gg * __double2float_rn(uu));
+    }
+    f64 sub = rho * rho * om;
+    f64 c1  = (sub != 0 && sub == sub) ? 1. / sub : 0.;
+    size_t p2 = 2 * (size_t) r;
+    P[p2]     = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / hh));
+    P[p2 + 1] = make_float4(lo32(x), lo32(y), lo32(z), cs);
+    H[p2]     = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(uu));
+    H[p2 + 1] = make_float4(hi32(Pr), __double2float_rn(c1), pack_bf16x2(lo32(vx), lo32(vy)),
+                            pack_bf16x2(lo32(vz), lo32(Pr)));
+}
+
 // sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a.  The next four entries
 // are fetched while the current four position records are in flight.
 __device__ __forceinline__ void density_sums_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
@@ -413,20 +468,25 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
     return cudaGetLastError();
 }
 
-cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
-                              f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,
-                              f64 C_force, const LocalFields &lf, const ExtAccel &ext) {
-    u32 N         = c.n_obj;
-    MixedSpace ms = mixed_space(c, N);
-    {
-        ProfScope ps(c, kProfGatherEos, N);
-        { k_stage_hydro<<<div_up(N, 256), 256, 0, c.stream>>>(N, nullptr, nullptr, nullptr, hs, pmass,
-                                                            c.f_pos.as<float4>(),
-                                                            c.f_aux0.as<float4>()); GBSPH_COUNTED; }
-    }
+cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
+                               const f64 *omega_local, f64 pmass, const EosParams &eos) {
+    StageEos se{eos.kind, eos.gamma, (float) (eos.gamma * (eos.gamma - 1)),
+                1.0 / (eos.r0 * eos.r0), (float) (eos.cs0 * eos.cs0), (float) -eos.q};
+    ProfScope ps(c, kProfGatherEos, N);
+    { k_gather_stage_mixed<<<div_up(N, 256), 256, 0, c.stream>>>(
+        c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf, omega_local, pmass, se,
+        c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.f_pos.as<float4>(),
+        c.f_aux0.as<float4>(), c.sh2.as<f64>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
+                              f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
+                              const LocalFields &lf, const ExtAccel &ext) {
+    MixedSpace ms = mixed_space(c, c.n_obj);
     MixedParams p = mixed_params(pmass, alpha_u, alpha_AV, beta_AV);
     ProfScope ps(c, kProfDerivs, rs.n);
-    { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, hs.h, hdt, C_cour,
+    { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, c.sh2.as<f64>(), hdt, C_cour,
                                                                  C_force, lf, ext,
                                                                  c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     return cudaGetLastError();

@@ -28,9 +28,15 @@ cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h
                             f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters,
                             f64 eps_p = 1e-6);
 cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
-cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
-                              f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 hdt, f64 C_cour,
-                              f64 C_force, const LocalFields &lf, const ExtAccel &ext);
+// the corrector's EOS + record staging for merged ranks 0..N-1 (replaces gather_eos64
+// + the FP64 rank-ordered copies in the mixed path; only h is kept in FP64, in c.sh2),
+// then the fused derivatives step, which reads the records, c.sh2 and the caller's
+// local fields
+cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
+                               const f64 *omega_local, f64 pmass, const EosParams &eos);
+cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
+                              f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
+                              const LocalFields &lf, const ExtAccel &ext);
 cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                                 f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
                                 f64 *du, f64 *vsig);

@@ -201,6 +201,31 @@ def test_neighbour_cache_slot_paths(gctx, M, budget, precision):
     assert np.array_equal(csr["entries"].cpu().numpy().view(np.uint32), oc["entries"])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_neighbour_cache_varying_h_vs_oracle(gctx, M, precision):
+    """Smoothing lengths spread over a factor 3 plus a dense clump with small h, free
+    boundary.  Stage 1 drops, per owner leaf, the leaves that none of its rows can pair
+    with (by the largest threshold of the rows it owns) and skips leaves that own no row;
+    the cache must still be the oracle's bit for bit."""
+    rng = np.random.default_rng(21)
+    s = _lattice(12, 0.1, 21)
+    n0 = len(s["h"])
+    clump = 0.5 + 0.03 * rng.standard_normal((2000, 3))
+    pos = np.concatenate([s["pos"], clump])
+    h = np.concatenate([s["h"] * rng.uniform(0.6, 1.8, n0),
+                        0.15 * s["h"][0] * rng.uniform(0.5, 2.0, 2000)])
+    n = len(h)
+    lo = np.nextafter(pos.min(0), -np.inf)
+    hi = np.nextafter(pos.max(0), np.inf)
+    t = M.Tree(gctx, pos, lo, hi, 3, h=h, htol=1.1)
+    csr = M.neighbour_cache(gctx, n, 1.1, precision)
+    o = O.Tree(pos, lo, hi, 3, h=h, htol=1.1)
+    oc = o.neigh_cache(pos, h, n, 1.1)
+    assert np.array_equal(csr["cnt"].cpu().numpy().view(np.uint32), oc["cnt"])
+    assert np.array_equal(csr["scanned"].cpu().numpy().view(np.uint32), oc["scanned"])
+    assert np.array_equal(csr["entries"].cpu().numpy().view(np.uint32), oc["entries"])
+
+
 def test_sort_properties_large(gctx, M):
     """Size-independent properties at 2^24 keys: sorted output, permutation, stable pairing."""
     n = 1 << 24
