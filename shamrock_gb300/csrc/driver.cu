@@ -58,7 +58,7 @@ Ctx::~Ctx() {
     for (cudaEvent_t e : prof.pool) cudaEventDestroy(e);
     DevBuf *bufs[] = {&scan_scratch, &d_scalars, &d_bbox, &keys, &sort_index, &flags_a, &flags_b,
                       &offsets, &reduc, &reduced, &lchild, &rchild, &lflag, &rflag, &endrange,
-                      &parent, &boxes, &visit, &fboxes, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
+                      &parent, &boxes, &visit, &fboxes, &fpairs, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
                       &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
                       &owner, &leaf_thr, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,

@@ -57,6 +57,13 @@ struct __align__(32) NodeBoxF {
     float4 hi;
 };
 
+// The two children of an internal node with their FP32 boxes (64 bytes, two 256-bit
+// loads), so a traversal tests both children of a node together; hi.w of each box
+// carries the child's node index (internal n, or leaf L - 1 + l) as raw bits.
+struct __align__(32) NodePairF {
+    NodeBoxF l, r;
+};
+
 // Live per-stage timing with CUDA events on the launching stream (off by default).
 enum ProfKind : int {
     kProfPredict = 0,
@@ -103,7 +110,7 @@ struct Ctx {
     int key_bits = 32;
     u32 n_obj = 0, morton_count = 0, leaf_count = 0;
     DevBuf keys, sort_index, flags_a, flags_b, offsets, reduc, reduced;
-    DevBuf lchild, rchild, lflag, rflag, endrange, parent, boxes, visit, fboxes;
+    DevBuf lchild, rchild, lflag, rflag, endrange, parent, boxes, visit, fboxes, fpairs;
     bool has_rint = false;
 
     // ---- rank-ordered copies of merged fields

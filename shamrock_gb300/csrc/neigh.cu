@@ -144,7 +144,26 @@ __global__ void k_boxes_f32(const NodeBox *__restrict__ b, u32 T, NodeBoxF *__re
                           __double2float_rn(v.hi[2]), 0.f);
 }
 
+__global__ void k_node_pairs(TreeView t, const NodeBoxF *__restrict__ fb, NodePairF *__restrict__ rec) {
+    u32 n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= t.off()) return; // internal nodes 0 .. L - 2
+    u32 l = t.left(n), r = t.right(n);
+    NodeBoxF bl = fb[l], br = fb[r];
+    bl.hi.w = __uint_as_float(l);
+    br.hi.w = __uint_as_float(r);
+    rec[n]  = NodePairF{bl, br};
+}
+
+// Stage 1 over the child-pair records.  A popped internal node loads both children's
+// boxes in one record and tests them together, pushing those that pass (right, then
+// left, so the left subtree is walked first); a popped leaf has passed and is
+// reported.  Every node is tested once, when its parent is expanded, so the leaves and
+// their order are those of dfs() with the same criterion; per step the traversal waits
+// on one record load instead of a box load and a child-index load per node.
+// leaf_thr (optional, see k_owner): a leaf owning no row gets an empty list, and a
+// candidate leaf that no owned row can pair with is dropped (the cache is unchanged).
 __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *__restrict__ fb,
+                                                    const NodePairF *__restrict__ rec,
                                                     u32 *__restrict__ cnt, u32 *__restrict__ off,
                                                     u32 *__restrict__ ent, u32 cap, Scalars *sc,
                                                     const u32 *__restrict__ leaf_thr) {
@@ -162,55 +181,61 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
         thr_own = __uint_as_float(tb);
     }
     LeafCrit crit(t, l);
-    bool ok;
-    if (fb) {
-        F8 fa = ldg256(&fb[t.off() + l]), fr = ldg256(&fb[0]);
-        const float4 alo = fa.a, ahi = fa.b, rlo = fr.a, rhi = fr.b;
-        float M = fmaxf(fmaxf(fmaxf(fabsf(rlo.x), fabsf(rlo.y)), fmaxf(fabsf(rlo.z), fabsf(rhi.x))),
-                        fmaxf(fabsf(rhi.y), fabsf(rhi.z)));
-        float band_abs = 1e-6f * M;
-        float4 llo = alo, lhi = ahi; // box of the node last tested
-        ok = dfs(
-            t,
-            [&](u32 node) {
-                F8 fn = ldg256(&fb[node]);
-                const float4 nlo = fn.a, nhi = fn.b;
-                llo = nlo;
-                lhi = nhi;
-                float sx = fmaxf(nlo.x - ahi.x, alo.x - nhi.x);
-                float sy = fmaxf(nlo.y - ahi.y, alo.y - nhi.y);
-                float sz = fmaxf(nlo.z - ahi.z, alo.z - nhi.z);
-                float sm = fmaxf(fmaxf(sx, sy), sz);
-                float R  = fmaxf(nlo.w, alo.w);
-                float band = band_abs + 1e-6f * R;
-                if (sm < R - band) return true;
-                if (sm > R + band) return false;
-                return crit(node);
-            },
-            [&](u32 leaf) {
-                if (leaf_thr) {
-                    // Exact pruning for stage 2 (the cache stays the same): every row
-                    // owned by this leaf lies in its box, so a pair (a, b) with b in
-                    // `leaf` has r_ab at least the Euclidean gap D between the boxes.
-                    // With thr_own >= thr_a of every owned row and (r_leaf R)^2 >= thr_b,
-                    // D^2 > max of the two makes every pair test fail.  The FP32 gaps
-                    // are shrunk by the rounding band and the bound carries a 1e-5
-                    // margin, so the skip is certain.
-                    float gx = fmaxf(fmaxf(llo.x - ahi.x, alo.x - lhi.x) - band_abs, 0.f);
-                    float gy = fmaxf(fmaxf(llo.y - ahi.y, alo.y - lhi.y) - band_abs, 0.f);
-                    float gz = fmaxf(fmaxf(llo.z - ahi.z, alo.z - lhi.z) - band_abs, 0.f);
-                    float d2 = gx * gx + gy * gy + gz * gz;
-                    float tb = fmaxf(thr_own, llo.w * llo.w * 1.000001f);
-                    if (d2 > tb * 1.00001f) return;
-                }
-                if (c < cap) ent[base + c] = leaf;
-                c++;
-            });
-    } else {
-        ok = dfs(t, crit, [&](u32 leaf) {
-            if (c < cap) ent[base + c] = leaf;
+    const u32 offn = t.off();
+    F8 fa = ldg256(&fb[offn + l]), fr = ldg256(&fb[0]);
+    const float4 alo = fa.a, ahi = fa.b, rlo = fr.a, rhi = fr.b;
+    float M = fmaxf(fmaxf(fmaxf(fabsf(rlo.x), fabsf(rlo.y)), fmaxf(fabsf(rlo.z), fabsf(rhi.x))),
+                    fmaxf(fabsf(rhi.y), fabsf(rhi.z)));
+    float band_abs = 1e-6f * M;
+    // the criterion with an FP32 decision outside the rounding band
+    auto test = [&](u32 node, const float4 &nlo, const float4 &nhi) -> bool {
+        float sx = fmaxf(nlo.x - ahi.x, alo.x - nhi.x);
+        float sy = fmaxf(nlo.y - ahi.y, alo.y - nhi.y);
+        float sz = fmaxf(nlo.z - ahi.z, alo.z - nhi.z);
+        float sm = fmaxf(fmaxf(sx, sy), sz);
+        float R  = fmaxf(nlo.w, alo.w);
+        float band = band_abs + 1e-6f * R;
+        if (sm < R - band) return true;
+        if (sm > R + band) return false;
+        return crit(node);
+    };
+    // Exact pruning for stage 2: every row owned by this leaf lies in its box, so a
+    // pair (a, b) with b in the candidate leaf has r_ab at least the Euclidean gap D
+    // between the boxes.  With thr_own >= thr_a of every owned row and
+    // (r_leaf R)^2 >= thr_b, D^2 > max of the two makes every pair test fail.  The FP32
+    // gaps are shrunk by the rounding band and the bound carries a 1e-5 margin, so the
+    // skip is certain.
+    auto keep = [&](const float4 &nlo, const float4 &nhi) -> bool {
+        if (!leaf_thr) return true;
+        float gx = fmaxf(fmaxf(nlo.x - ahi.x, alo.x - nhi.x) - band_abs, 0.f);
+        float gy = fmaxf(fmaxf(nlo.y - ahi.y, alo.y - nhi.y) - band_abs, 0.f);
+        float gz = fmaxf(fmaxf(nlo.z - ahi.z, alo.z - nhi.z) - band_abs, 0.f);
+        float d2 = gx * gx + gy * gy + gz * gz;
+        float tb = fmaxf(thr_own, nlo.w * nlo.w * 1.000001f);
+        return !(d2 > tb * 1.00001f);
+    };
+    u32 stack[kStack];
+    int top = 0;
+    bool ok = true;
+    if (test(0, rlo, rhi) && (offn > 0 || keep(rlo, rhi))) stack[top++] = 0;
+    while (top > 0) {
+        const u32 n = stack[--top];
+        if (n >= offn) {
+            if (c < cap) ent[base + c] = n - offn;
             c++;
-        });
+            continue;
+        }
+        const F8 bl = ldg256(&rec[n].l), br = ldg256(&rec[n].r);
+        const u32 li = __float_as_uint(bl.b.w), ri = __float_as_uint(br.b.w);
+        bool pl = test(li, bl.a, bl.b), pr = test(ri, br.a, br.b);
+        if (pl && li >= offn) pl = keep(bl.a, bl.b);
+        if (pr && ri >= offn) pr = keep(br.a, br.b);
+        if (top + 2 > kStack) {
+            ok = false;
+            break;
+        }
+        if (pr) stack[top++] = ri;
+        if (pl) stack[top++] = li;
     }
     if (!ok) atomicOr(&sc->flags, kFlagStackOverflow);
     if (c > cap) {
@@ -239,39 +264,58 @@ __global__ void k_rows(const u32 *__restrict__ sort_index, const u8 *__restrict_
 }
 
 // ---- owner leaf: max leaf index whose box contains the point (inclusive bounds),
-// i.e. the last leaf the reference's left-first DFS reports (NeighbourCache.cpp:419-443)
+// i.e. the last leaf the reference's left-first DFS reports (NeighbourCache.cpp:419-443).
+// Right-first traversal over the child-pair records (the first leaf reached is the
+// largest); containment is decided in FP32 outside a rounding band, else in FP64.
 // leaf_thr (optional): per leaf, the FP32 bits (rounded up) of the largest pair-test
 // threshold thr_a = ((h_a htol)^2) R^2 over the rows it owns, 0 for a leaf owning none.
-__global__ void k_owner(TreeView t, const u32 *__restrict__ row_rank, u32 n_rows,
-                        const f64 *__restrict__ sx, const f64 *__restrict__ sy,
-                        const f64 *__restrict__ sz, u32 *__restrict__ owner, u32 *__restrict__ flags,
-                        const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ leaf_thr) {
+__global__ void __launch_bounds__(128) k_owner(TreeView t, const NodeBoxF *__restrict__ fb,
+                                               const NodePairF *__restrict__ rec,
+                                               const u32 *__restrict__ row_rank, u32 n_rows,
+                                               const f64 *__restrict__ sx, const f64 *__restrict__ sy,
+                                               const f64 *__restrict__ sz, u32 *__restrict__ owner,
+                                               u32 *__restrict__ flags, const f64 *__restrict__ sh,
+                                               f64 h_tol, u32 *__restrict__ leaf_thr) {
     u32 row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n_rows) return;
     u32 r    = row_rank[row];
     f64 p[3] = {sx[r], sy[r], sz[r]};
+    const float px = __double2float_rn(p[0]), py = __double2float_rn(p[1]),
+                pz = __double2float_rn(p[2]);
+    const F8 fr = ldg256(&fb[0]);
+    float M = fmaxf(fmaxf(fmaxf(fabsf(fr.a.x), fabsf(fr.a.y)), fmaxf(fabsf(fr.a.z), fabsf(fr.b.x))),
+                    fmaxf(fabsf(fr.b.y), fabsf(fr.b.z)));
+    const float band = 1e-6f * M;
+    auto inside = [&](u32 node, const float4 &lo, const float4 &hi) -> bool {
+        float m = fminf(fminf(fminf(px - lo.x, py - lo.y), fminf(pz - lo.z, hi.x - px)),
+                        fminf(hi.y - py, hi.z - pz));
+        if (m > band) return true;
+        if (m < -band) return false;
+        f64 l64[3], h64[3], rr;
+        load_box(&t.boxes[node], l64, h64, rr);
+        return (l64[0] <= p[0]) && (p[0] <= h64[0]) && (l64[1] <= p[1]) && (p[1] <= h64[1])
+               && (l64[2] <= p[2]) && (p[2] <= h64[2]);
+    };
+    const u32 offn = t.off();
     u32 stack[kStack];
-    int top      = 0;
-    stack[top++] = 0;
-    u32 off      = t.off();
-    u32 found    = kNone;
+    int top   = 0;
+    u32 found = kNone;
+    if (inside(0, fr.a, fr.b)) stack[top++] = 0;
     while (top > 0) {
-        u32 node = stack[--top];
-        f64 lo[3], hi[3], rr;
-        load_box(&t.boxes[node], lo, hi, rr);
-        bool in = (lo[0] <= p[0]) && (p[0] <= hi[0]) && (lo[1] <= p[1]) && (p[1] <= hi[1])
-                  && (lo[2] <= p[2]) && (p[2] <= hi[2]);
-        if (!in) continue;
-        if (node >= off) {
-            found = node - off;
+        const u32 n = stack[--top];
+        if (n >= offn) {
+            found = n - offn;
             break;
         }
+        const F8 bl = ldg256(&rec[n].l), br = ldg256(&rec[n].r);
+        const u32 li = __float_as_uint(bl.b.w), ri = __float_as_uint(br.b.w);
+        const bool cl = inside(li, bl.a, bl.b), cr = inside(ri, br.a, br.b);
         if (top + 2 > kStack) {
             atomicOr(flags, kFlagStackOverflow);
             break;
         }
-        stack[top++] = t.left(node);
-        stack[top++] = t.right(node);
+        if (cl) stack[top++] = li;
+        if (cr) stack[top++] = ri;
     }
     if (found == kNone) {
         atomicOr(flags, kFlagOwnerMissing);
@@ -445,6 +489,10 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     cudaStream_t s = c.stream;
     cudaError_t e;
     u32 L = c.leaf_count, n = c.n_local;
+    if (L == 0) {
+        c.err = "neighbour cache: the tree has no leaves";
+        return cudaErrorInvalidValue;
+    }
     TreeView t = view(c);
     Scalars *dsc = c.d_scalars.as<Scalars>();
     if ((e = c.leaf_cnt.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
@@ -461,26 +509,25 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     const u64 budget = c.slot_budget ? c.slot_budget : kMaxSlotBytes;
     auto slots_ok = [&](u64 rows, u32 cap) { return rows * cap < 0xffffffffull && rows * cap * 4 <= budget; };
     const bool s1_one_pass = slots_ok(L, c.leaf_cap);
-    const NodeBoxF *fb = nullptr;
-    if (P) {
-        u32 T = 2 * L - 1;
-        if ((e = c.fboxes.ensure(sizeof(NodeBoxF) * (size_t) T, s)) != cudaSuccess) return e;
-        { k_boxes_f32<<<div_up(T, 256), 256, 0, s>>>(c.boxes.as<NodeBox>(), T, c.fboxes.as<NodeBoxF>()); GBSPH_COUNTED; }
-        fb = c.fboxes.as<NodeBoxF>();
-    }
-    // Owner leaves first.  With FP32 boxes it also records, per leaf, the largest
-    // threshold of the rows it owns, which lets stage 1 drop leaves that no owned row
-    // can pair with (and skip leaves that own no row); the cache is unchanged.
+    // FP32 node boxes and the child-pair records the traversals read (the FP64 boxes
+    // decide inside the rounding band)
+    const u32 T = 2 * L - 1;
+    if ((e = c.fboxes.ensure(sizeof(NodeBoxF) * (size_t) T, s)) != cudaSuccess) return e;
+    if ((e = c.fpairs.ensure(sizeof(NodePairF) * (size_t) L, s)) != cudaSuccess) return e;
+    { k_boxes_f32<<<div_up(T, 256), 256, 0, s>>>(c.boxes.as<NodeBox>(), T, c.fboxes.as<NodeBoxF>()); GBSPH_COUNTED; }
+    const NodeBoxF *fb = c.fboxes.as<NodeBoxF>();
+    const NodePairF *rec = c.fpairs.as<NodePairF>();
+    if (L > 1) { k_node_pairs<<<div_up(L - 1, 256), 256, 0, s>>>(t, fb, c.fpairs.as<NodePairF>()); GBSPH_COUNTED; }
+    // Owner leaves first: they also record, per leaf, the largest threshold of the rows
+    // it owns, which lets stage 1 drop leaves that no owned row can pair with (and skip
+    // leaves that own no row); the cache is unchanged.
     if ((e = c.owner.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
-    u32 *leaf_thr = nullptr;
-    if (fb) {
-        if ((e = c.leaf_thr.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(c.leaf_thr.p, 0, sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
-        leaf_thr = c.leaf_thr.as<u32>();
-    }
+    if ((e = c.leaf_thr.ensure(sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c.leaf_thr.p, 0, sizeof(u32) * (size_t) L, s)) != cudaSuccess) return e;
+    u32 *leaf_thr = c.leaf_thr.as<u32>();
     if (n) {
         ProfScope ps(c, kProfOwner, n);
-        { k_owner<<<div_up(n, 128), 128, 0, s>>>(t, c.row_rank.as<u32>(), n, c.sx.as<f64>(),
+        { k_owner<<<div_up(n, 128), 128, 0, s>>>(t, fb, rec, c.row_rank.as<u32>(), n, c.sx.as<f64>(),
                                                c.sy.as<f64>(), c.sz.as<f64>(), c.owner.as<u32>(),
                                                &dsc->flags, c.sh.as<f64>(), h_tol, leaf_thr); GBSPH_COUNTED; }
     }
@@ -488,7 +535,7 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         cudaError_t err = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * c.leaf_cap + 1), s);
         if (err != cudaSuccess) return err;
         ProfScope ps(c, kProfStage1, L);
-        { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
+        { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, rec, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
                                                     c.leaf_ent.as<u32>(), c.leaf_cap, dsc, leaf_thr); GBSPH_COUNTED; }
         return cudaGetLastError();
     };
