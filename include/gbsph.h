@@ -177,6 +177,8 @@ int gbsph_tree_query(gbsph_ctx *ctx, const double *qx, const double *qy, const d
 int gbsph_neighbour_cache(gbsph_ctx *ctx, uint32_t n_local, double htol, uint32_t precision,
                           void *stream);
 
+/* total_host: stage-2 entries of the last cache.  leaf_total_host: stage-1 rank ranges
+ * when the last build ran the two-pass stage 1 (slots past the budget), else 0. */
 int gbsph_cache_size(gbsph_ctx *ctx, uint64_t *total_host, uint64_t *leaf_total_host);
 
 /* The cache in the reference's ObjectCache layout (TreeTraversal.hpp:375-485):

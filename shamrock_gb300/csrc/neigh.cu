@@ -4,7 +4,9 @@
 //   criteria shamtree/include/shamtree/kernels/geometry_utils.hpp:62-135,
 //   CSR layout shamtree/include/shamtree/TreeTraversal.hpp:375-526.
 //
-// Stage 1: leaf -> candidate leaves (extended-AABB overlap, both directions).
+// Stage 1: leaf -> candidate leaves (extended-AABB overlap, both directions), stored
+//          as rank ranges: consecutive leaves cover consecutive ranks, so runs of
+//          consecutive candidates merge and stage 2 walks fewer, longer runs.
 // Owner:   local particle -> leaf (the last leaf, in DFS order, whose box holds it).
 // Stage 2: local particle -> interacting particles, pair test
 //          !(r^2 > (h_a htol)^2 R^2 && r^2 > (h_b htol)^2 R^2).
@@ -74,6 +76,34 @@ __device__ __forceinline__ bool dfs(const TreeView &t, Crit &&crit, OnLeaf &&on_
     return true;
 }
 
+// Candidate leaves arrive in ascending order; a leaf following the previous run
+// directly extends it.  A run of leaves [l0, l1) is stored as its rank range
+// [reduc[l0], reduc[l1]).  `c` counts runs; only the first `cap` are stored.
+struct RangeWriter {
+    uint2 *out;
+    const u32 *reduc;
+    u32 base, cap, c;
+    uint2 cur;
+    bool open;
+    __device__ RangeWriter(uint2 *o, const u32 *rd, u32 b, u32 cp)
+        : out(o), reduc(rd), base(b), cap(cp), c(0), open(false) {}
+    __device__ __forceinline__ void add(u32 r0, u32 r1) {
+        if (open && cur.y == r0) {
+            cur.y = r1;
+            return;
+        }
+        flush();
+        cur  = make_uint2(r0, r1);
+        open = true;
+    }
+    __device__ __forceinline__ void flush() {
+        if (!open) return;
+        if (out && c < cap) out[base + c] = make_uint2(reduc[cur.x], reduc[cur.y]);
+        c++;
+        open = false;
+    }
+};
+
 // ---- stage 1 criterion (NeighbourCache.cpp:289-334)
 __device__ __forceinline__ bool cella_neigh_b(const f64 amin[3], const f64 amax[3],
                                               const f64 bmin[3], const f64 bmax[3]) {
@@ -109,22 +139,25 @@ struct LeafCrit {
     }
 };
 
+// exact two-pass stage 1: range counts, then ranges at the scanned offsets
 __global__ void k_leaf_count(TreeView t, u32 *__restrict__ cnt, u32 *__restrict__ flags) {
     u32 l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= t.L) return;
     LeafCrit crit(t, l);
-    u32 c   = 0;
-    bool ok = dfs(t, crit, [&](u32) { c++; });
+    RangeWriter w(nullptr, t.reduc, 0, 0);
+    bool ok = dfs(t, crit, [&](u32 leaf) { w.add(leaf, leaf + 1); });
+    w.flush();
     if (!ok) atomicOr(flags, kFlagStackOverflow);
-    cnt[l] = c;
+    cnt[l] = w.c;
 }
 
-__global__ void k_leaf_fill(TreeView t, const u32 *__restrict__ off, u32 *__restrict__ ent) {
+__global__ void k_leaf_fill(TreeView t, const u32 *__restrict__ off, uint2 *__restrict__ ent) {
     u32 l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= t.L) return;
     LeafCrit crit(t, l);
-    u32 w = off[l];
-    dfs(t, crit, [&](u32 leaf) { ent[w++] = leaf; });
+    RangeWriter w(ent, t.reduc, off[l], 0xffffffffu);
+    dfs(t, crit, [&](u32 leaf) { w.add(leaf, leaf + 1); });
+    w.flush();
 }
 
 // ---- stage 1, one pass into `cap` slots per leaf, optional FP32 pre-test.
@@ -165,11 +198,11 @@ __global__ void k_node_pairs(TreeView t, const NodeBoxF *__restrict__ fb, NodePa
 __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *__restrict__ fb,
                                                     const NodePairF *__restrict__ rec,
                                                     u32 *__restrict__ cnt, u32 *__restrict__ off,
-                                                    u32 *__restrict__ ent, u32 cap, Scalars *sc,
+                                                    uint2 *__restrict__ ent, u32 cap, Scalars *sc,
                                                     const u32 *__restrict__ leaf_thr) {
     u32 l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= t.L) return;
-    u32 c = 0, base = l * cap;
+    u32 base = l * cap;
     float thr_own = 0.f;
     if (leaf_thr) {
         const u32 tb = leaf_thr[l];
@@ -217,12 +250,12 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
     u32 stack[kStack];
     int top = 0;
     bool ok = true;
+    RangeWriter w(ent, t.reduc, base, cap);
     if (test(0, rlo, rhi) && (offn > 0 || keep(rlo, rhi))) stack[top++] = 0;
     while (top > 0) {
         const u32 n = stack[--top];
         if (n >= offn) {
-            if (c < cap) ent[base + c] = n - offn;
-            c++;
+            w.add(n - offn, n - offn + 1);
             continue;
         }
         const F8 bl = ldg256(&rec[n].l), br = ldg256(&rec[n].r);
@@ -237,6 +270,8 @@ __global__ void __launch_bounds__(128) k_leaf_lists(TreeView t, const NodeBoxF *
         if (pr) stack[top++] = ri;
         if (pl) stack[top++] = li;
     }
+    w.flush();
+    const u32 c = w.c;
     if (!ok) atomicOr(&sc->flags, kFlagStackOverflow);
     if (c > cap) {
         atomicOr(&sc->flags, kFlagLeafCap);
@@ -346,7 +381,7 @@ template<int MODE, bool F32>
 __global__ void __launch_bounds__(256) k_part_cache(
     const u32 *__restrict__ row_rank, u32 n_rows, const u32 *__restrict__ owner,
     const u32 *__restrict__ leaf_cnt, const u32 *__restrict__ leaf_off,
-    const u32 *__restrict__ leaf_ent, const u32 *__restrict__ reduc, const float4 *__restrict__ P,
+    const uint2 *__restrict__ leaf_ent, const float4 *__restrict__ P,
     const f64 *__restrict__ sx, const f64 *__restrict__ sy, const f64 *__restrict__ sz,
     const f64 *__restrict__ sh, f64 h_tol, u32 *__restrict__ cnt, u32 *__restrict__ off,
     u32 *__restrict__ ent, Scalars *sc, u32 cap) {
@@ -367,10 +402,26 @@ __global__ void __launch_bounds__(256) k_part_cache(
         u32 leaf = owner[row];
         u32 k0 = leaf_off[leaf], k1 = k0 + leaf_cnt[leaf];
         u32 w = (MODE == kFill) ? off[row] : ((MODE == kOnePass) ? row * cap : 0);
-        for (u32 k = k0; k < k1; k++) {
-            u32 lb = leaf_ent[k];
-            u32 r0 = reduc[lb], r1 = reduc[lb + 1];
-            for (u32 rb = r0; rb < r1; rb++) {
+        // one flat loop over the row's candidates (rows of a warp with different owner
+        // leaves then stay converged); the next range is fetched one range ahead
+        uint2 g  = (k0 < k1) ? leaf_ent[k0] : make_uint2(0, 0);
+        u32 k    = k0 + 1;
+        uint2 gn = (k < k1) ? leaf_ent[k] : g;
+        u32 rb   = g.x;
+        bool more = true;
+        while (true) {
+            while (rb >= g.y) {
+                if (k >= k1) {
+                    more = false;
+                    break;
+                }
+                g  = gn;
+                rb = g.x;
+                k++;
+                if (k < k1) gn = leaf_ent[k];
+            }
+            if (!more) break;
+            {
                 int decided = -1;
                 if (F32) {
                     F8 pb = ldg256(&P[2 * (size_t) rb]);
@@ -399,6 +450,7 @@ __global__ void __launch_bounds__(256) k_part_cache(
                     c++;
                 }
             }
+            rb++;
         }
         if (MODE != kFill) cnt[row] = c;
         if (MODE == kCount) off[row] = (c + 3u) & ~3u;
@@ -507,8 +559,10 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     if ((e = cudaMemsetAsync(&dsc->flags, 0, 3 * sizeof(u32), s)) != cudaSuccess) return e;
     if (c.leaf_cap == 0) c.leaf_cap = kLeafCap;
     const u64 budget = c.slot_budget ? c.slot_budget : kMaxSlotBytes;
-    auto slots_ok = [&](u64 rows, u32 cap) { return rows * cap < 0xffffffffull && rows * cap * 4 <= budget; };
-    const bool s1_one_pass = slots_ok(L, c.leaf_cap);
+    auto slots_ok = [&](u64 rows, u32 cap, u64 esize = 4) {
+        return rows * cap < 0xffffffffull && rows * cap * esize <= budget;
+    };
+    const bool s1_one_pass = slots_ok(L, c.leaf_cap, sizeof(uint2));
     // FP32 node boxes and the child-pair records the traversals read (the FP64 boxes
     // decide inside the rounding band)
     const u32 T = 2 * L - 1;
@@ -532,11 +586,11 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
                                                &dsc->flags, c.sh.as<f64>(), h_tol, leaf_thr); GBSPH_COUNTED; }
     }
     auto stage1 = [&]() -> cudaError_t {
-        cudaError_t err = c.leaf_ent.ensure(sizeof(u32) * ((size_t) L * c.leaf_cap + 1), s);
+        cudaError_t err = c.leaf_ent.ensure(sizeof(uint2) * ((size_t) L * c.leaf_cap + 1), s);
         if (err != cudaSuccess) return err;
         ProfScope ps(c, kProfStage1, L);
         { k_leaf_lists<<<div_up(L, 128), 128, 0, s>>>(t, fb, rec, c.leaf_cnt.as<u32>(), c.leaf_off.as<u32>(),
-                                                    c.leaf_ent.as<u32>(), c.leaf_cap, dsc, leaf_thr); GBSPH_COUNTED; }
+                                                    c.leaf_ent.as<uint2>(), c.leaf_cap, dsc, leaf_thr); GBSPH_COUNTED; }
         return cudaGetLastError();
     };
     if (s1_one_pass) {
@@ -555,7 +609,7 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     c.leaf_csr_total = 0;
     if (c.h_scalars->flags & kFlagLeafCap) {
         const u32 cap = (c.h_scalars->leaf_cnt_max + 31u) & ~31u;
-        const bool fits = s1_one_pass && slots_ok(L, cap);
+        const bool fits = s1_one_pass && slots_ok(L, cap, sizeof(uint2));
         if ((e = cudaMemsetAsync(&dsc->flags, 0, sizeof(u32), s)) != cudaSuccess) return e;
         if (fits) {
             // one pass again with slots that hold the largest list
@@ -570,8 +624,8 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
                 return e;
             if ((e = sync_scalars(c)) != cudaSuccess) return e;
             c.leaf_csr_total = c.h_scalars->total;
-            if ((e = c.leaf_ent.ensure(sizeof(u32) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
-            { k_leaf_fill<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_off.as<u32>(), c.leaf_ent.as<u32>()); GBSPH_COUNTED; }
+            if ((e = c.leaf_ent.ensure(sizeof(uint2) * (c.leaf_csr_total + 1), s)) != cudaSuccess) return e;
+            { k_leaf_fill<<<div_up(L, 128), 128, 0, s>>>(t, c.leaf_off.as<u32>(), c.leaf_ent.as<uint2>()); GBSPH_COUNTED; }
         }
     }
 
@@ -590,12 +644,12 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         if (P) {
             { k_part_cache<MODE, true><<<div_up(n, 256), 256, 0, s>>>(
                 c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
-                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), P, c.sx.as<f64>(),
+                c.leaf_off.as<u32>(), c.leaf_ent.as<uint2>(), P, c.sx.as<f64>(),
                 c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off, ent, dsc, c.row_cap); GBSPH_COUNTED; }
         } else {
             { k_part_cache<MODE, false><<<div_up(n, 256), 256, 0, s>>>(
                 c.row_rank.as<u32>(), n, c.owner.as<u32>(), c.leaf_cnt.as<u32>(),
-                c.leaf_off.as<u32>(), c.leaf_ent.as<u32>(), c.reduc.as<u32>(), nullptr,
+                c.leaf_off.as<u32>(), c.leaf_ent.as<uint2>(), nullptr,
                 c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.sh.as<f64>(), h_tol, cnt, off,
                 ent, dsc, c.row_cap); GBSPH_COUNTED; }
         }
