@@ -115,6 +115,23 @@ def test_morton_sort_vs_oracle(gctx, M, n, key_bits):
     assert np.array_equal(perm.cpu().numpy().view(np.uint32), operm)
 
 
+@pytest.mark.parametrize("n,key_bits,span", [(1 << 12, 32, 5), (1 << 13, 32, 7), (1 << 17, 32, 50),
+                                             (1 << 16, 64, 30), (1 << 20, 32, 1000)])
+def test_sort_ties_vs_oracle(gctx, M, n, key_bits, span):
+    """Keys drawn from a few values: which of equal keys goes first is fixed by the
+    bitonic network's compare-exchanges, so the permutation must be the oracle's."""
+    import torch
+
+    rng = np.random.default_rng(n + span)
+    k = rng.integers(0, span, n)
+    dt = torch.int32 if key_bits == 32 else torch.int64
+    keys = torch.as_tensor(k.astype(np.int32 if key_bits == 32 else np.int64), dtype=dt, device="cuda")
+    sk, perm = M.sort_by_key(gctx, keys, key_bits=key_bits)
+    ok, operm = O.bitonic_sort(k.astype(np.uint32 if key_bits == 32 else np.uint64))
+    assert np.array_equal(M.unsigned(sk, key_bits), ok)
+    assert np.array_equal(perm.cpu().numpy().view(np.uint32), operm)
+
+
 @pytest.mark.parametrize("n,level", [(2, 3), (100, 0), (5000, 1), (5000, 3), (120000, 3), (120001, 2)])
 def test_tree_vs_oracle(gctx, M, n, level):
     rng = np.random.default_rng(n + level)
