@@ -117,6 +117,9 @@ struct OpMinU64 {
 struct OpAddF64 {
     __device__ f64 operator()(f64 a, f64 b) const { return a + b; }
 };
+struct OpAddF32 {
+    __device__ float operator()(float a, float b) const { return a + b; }
+};
 struct OpAddU32 {
     __device__ u32 operator()(u32 a, u32 b) const { return a + b; }
 };

@@ -11,8 +11,16 @@
 // entries behind them, so each batch waits on one round trip.  Sums are accumulated
 // per batch in plain FP32 and the batch sums are Kahan-compensated.  This unit is
 // compiled with approximate FP32 division and square root (about 2 ulp).
+//
+// GB300 executes FP64 at a small fraction of its FP32 rate, so the per-particle work
+// around the pair loops avoids FP64 wherever the result is stored in FP32 anyway or is
+// dimensionless: hi/lo splits use integer operations (split64.cuh), 1/h is an FP32
+// reciprocal, the Newton step and Omega are computed from the dimensionless ratios
+// rho_sum / rho_h and h (d rho / dh) / rho_h, and the CFL step runs in FP32.  FP64 stays
+// on the state (h, x, v, u, a) and on pressure, whose hi/lo pair carries it beyond FP32.
 
 #include "sph_mixed.cuh"
+#include "split64.cuh"
 
 #include <cuda_bf16.h>
 
@@ -39,6 +47,17 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 }
 __device__ __forceinline__ float hi32(f64 v) { return __double2float_rn(v); }
 __device__ __forceinline__ float lo32(f64 v) { return __double2float_rn(v - (f64) __double2float_rn(v)); }
+// 1/v from the FP32 reciprocal refined by one FP64 Newton step (relative error ~1e-14,
+// so its FP32 rounding is the correctly rounded 1/v but for rare ties); plain FP64
+// division where the FP32 reciprocal leaves the normal range
+__device__ __forceinline__ f64 rcp64(f64 v) {
+    const float y0 = __frcp_rn(__double2float_rn(v));
+    if (!(fabsf(y0) < 3.0e38f && fabsf(y0) > 1.0e-37f)) return 1.0 / v;
+    const f64 y = (f64) y0;
+    return y * (2.0 - v * y);
+}
+// kNorm3d / hfact^3: rho_sum / rho_h = kC sum f(q), h (d rho/dh) / rho_h = -kC sum (3f + q f')
+constexpr float kDensRatio = (float) (kNorm3d / (kHfact * kHfact * kHfact));
 
 // Two residuals in one 32-bit word as bfloat16 (8 exponent bits: the range of a float,
 // so no residual underflows): with hi = fl32(v) the pair hi + bf16(lo) carries v to
@@ -82,11 +101,15 @@ __global__ void k_stage_pos(u32 N, const f64 *__restrict__ sx, const f64 *__rest
                             float4 *__restrict__ P) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
-    f64 x = sx[r], y = sy[r], z = sz[r];
-    f64 rint = __dmul_rn(sh[r], h_tol);
+    float xh, xl, yh, yl, zh, zl;
+    split64(sx[r], xh, xl);
+    split64(sy[r], yh, yl);
+    split64(sz[r], zh, zl);
+    const f64 h = sh[r];
+    f64 rint = __dmul_rn(h, h_tol);
     f64 thr  = __dmul_rn(__dmul_rn(rint, rint), kRkern * kRkern);
-    P[2 * (size_t) r]     = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / sh[r]));
-    P[2 * (size_t) r + 1] = make_float4(lo32(x), lo32(y), lo32(z), __double2float_rn(thr));
+    P[2 * (size_t) r]     = make_float4(xh, yh, zh, __double2float_rn(rcp64(h)));
+    P[2 * (size_t) r + 1] = make_float4(xl, yl, zl, __double2float_rn(thr));
 }
 
 // hydro staging from FP64 fields in the entry index space
@@ -125,10 +148,11 @@ __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__res
 // evaluated in FP32 (relative error ~2e-7, the size of the records' own rounding); rho,
 // P and 1/(rho^2 Omega) stay FP64 until they are split into the record.
 struct StageEos {
-    u32 kind;     // 0 adiabatic, 1 locally isothermal LP07
-    f64 gamma;
-    float gg;     // gamma (gamma - 1)
-    f64 inv_r0sq; // 1 / r0^2
+    u32 kind;       // 0 adiabatic, 1 locally isothermal LP07
+    f64 gm1;        // gamma - 1
+    f64 mh3;        // m hfact^3: rho = mh3 / h^3
+    float gg;       // gamma (gamma - 1)
+    float inv_r0sq; // 1 / r0^2
     float cs0sq, mq;
 };
 
@@ -144,29 +168,37 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
     u32 src = id < n_local ? id : ghost_src[id - n_local];
     size_t iv = (size_t) src * lf.vs;
     f64 hh = lf.h[src], uu = lf.u[src], om = omega[src];
-    f64 vx = lf.vx[iv], vy = lf.vy[iv], vz = lf.vz[iv];
-    f64 x = sx[r], y = sy[r], z = sz[r];
+    float xh, xl, yh, yl, zh, zl, vxh, vxl, vyh, vyl, vzh, vzl;
+    split64(sx[r], xh, xl);
+    split64(sy[r], yh, yl);
+    split64(sz[r], zh, zl);
+    split64(lf.vx[iv], vxh, vxl);
+    split64(lf.vy[iv], vyh, vyl);
+    split64(lf.vz[iv], vzh, vzl);
     h_rank[r] = hh;
-    f64 rho   = rho_h64(pmass, hh);
+    const f64 hinv    = rcp64(hh);
+    const float hinv_f = __double2float_rn(hinv);
+    const f64 rho      = eos.mh3 * hinv * hinv * hinv;
     f64 Pr;
     float cs;
     if (eos.kind == 1) {
-        float ratio = __double2float_rn((x * x + y * y + z * z) * eos.inv_r0sq);
+        float ratio = (xh * xh + yh * yh + zh * zh) * eos.inv_r0sq;
         float cs_sq = eos.cs0sq * powf(ratio, eos.mq);
         Pr          = (f64) cs_sq * rho;
         cs          = sqrtf(cs_sq);
     } else {
-        Pr = (eos.gamma - 1) * rho * uu;
+        Pr = eos.gm1 * rho * uu;
         cs = sqrtf(eos.gg * __double2float_rn(uu));
     }
-    f64 sub = rho * rho * om;
-    f64 c1  = (sub != 0 && sub == sub) ? 1. / sub : 0.;
+    const f64 sub  = rho * rho * om;
+    const float c1 = (sub != 0 && sub == sub) ? __double2float_rn(rcp64(sub)) : 0.f;
+    float Ph, Pl;
+    split64(Pr, Ph, Pl);
     size_t p2 = 2 * (size_t) r;
-    P[p2]     = make_float4(hi32(x), hi32(y), hi32(z), __double2float_rn(1.0 / hh));
-    P[p2 + 1] = make_float4(lo32(x), lo32(y), lo32(z), cs);
-    H[p2]     = make_float4(hi32(vx), hi32(vy), hi32(vz), __double2float_rn(uu));
-    H[p2 + 1] = make_float4(hi32(Pr), __double2float_rn(c1), pack_bf16x2(lo32(vx), lo32(vy)),
-                            pack_bf16x2(lo32(vz), lo32(Pr)));
+    P[p2]     = make_float4(xh, yh, zh, hinv_f);
+    P[p2 + 1] = make_float4(xl, yl, zl, cs);
+    H[p2]     = make_float4(vxh, vyh, vzh, __double2float_rn(uu));
+    H[p2 + 1] = make_float4(Ph, c1, pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, Pl));
 }
 
 // sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a.  The next four entries
@@ -217,25 +249,31 @@ __global__ void __launch_bounds__(256, 4) k_h_iterate_mixed(RowSpace rs, MixedSp
     if (t < rs.n) {
         u32 a  = rs.row_rank ? rs.row_rank[t] : t;
         u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
-        const f64 h_max_evol_m = 1 / h_evol_iter_max;
-        f64 ha_0 = h_old[t], h_a = h_new[t], e = eps[t];
+        // The Newton step of IterateSmoothingLengthDensity in dimensionless form:
+        //   new_h = h - (rho_sum - rho_h) / (drho/dh + 3 rho_h / h) = h (1 - (A - 1) / (B + 3))
+        // with A = rho_sum / rho_h and B = h (drho/dh) / rho_h, both FP32 sums times
+        // kNorm3d / hfact^3; the relative update is FP32, h itself stays FP64.
+        const float it_max = (float) h_evol_iter_max, it_min = 1.f / it_max;
+        const f64 ha_0 = h_old[t], h_lim = ha_0 * h_evol_max;
+        const float inv_h0 = __frcp_rn(__double2float_rn(ha_0));
+        f64 h_a = h_new[t], e = eps[t];
         for (u32 it = 0; it < iters; it++) {
             if (!(e > eps_p)) break;
             used++;
             float sf, sg;
-            density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(1.0 / h_a), sf, sg);
-            f64 h3      = h_a * h_a * h_a;
-            f64 rho_sum = pmass * kNorm3d * (f64) sf / h3;
-            f64 sumdWdh = -pmass * kNorm3d * (f64) sg / (h3 * h_a);
-            f64 rho_ha  = rho_h64(pmass, h_a);
-            f64 new_h   = h_a - (rho_sum - rho_ha) / (sumdWdh + 3 * rho_ha / h_a);
-            if (new_h < h_a * h_max_evol_m) new_h = h_max_evol_m * h_a;
-            if (new_h > h_a * h_evol_iter_max) new_h = h_evol_iter_max * h_a;
-            if (new_h < ha_0 * h_evol_max) {
-                e   = fabs(new_h - h_a) / ha_0;
+            const float hf = __double2float_rn(h_a);
+            density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(rcp64(h_a)), sf, sg);
+            const float A = kDensRatio * sf, B = -kDensRatio * sg;
+            float d = __fdiv_rn(A - 1.f, B + 3.f); // new_h = h (1 - d)
+            float f = 1.f - d;
+            if (f < it_min) d = 1.f - it_min;
+            if (f > it_max) d = 1.f - it_max;
+            const f64 new_h = h_a - h_a * (f64) d;
+            if (new_h < h_lim) {
+                e   = (f64) (fabsf(d) * hf * inv_h0);
                 h_a = new_h;
             } else {
-                h_a = ha_0 * h_evol_max;
+                h_a = h_lim;
                 e   = -1;
             }
         }
@@ -261,12 +299,10 @@ __global__ void __launch_bounds__(256) k_omega_mixed(RowSpace rs, MixedSpace ms,
     if (t >= rs.n) return;
     u32 a  = rs.row_rank ? rs.row_rank[t] : t;
     u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
-    f64 h_a = h_row[t];
     float sf, sg;
-    density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(1.0 / h_a), sf, sg);
-    f64 sumdWdh = -pmass * kNorm3d * (f64) sg / (h_a * h_a * h_a * h_a);
-    f64 rho_ha  = rho_h64(pmass, h_a);
-    omega_local[rs.row_local ? rs.row_local[t] : t] = 1 + (h_a / (3 * rho_ha)) * sumdWdh;
+    density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(rcp64(h_row[t])), sf, sg);
+    // Omega = 1 + h / (3 rho_h) drho/dh = 1 + B / 3, B = -kNorm3d / hfact^3 sum (3f + q f')
+    omega_local[rs.row_local ? rs.row_local[t] : t] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
 }
 
 struct MixedParams {
@@ -377,7 +413,7 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
                                                            ExtAccel ext, Scalars *sc) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     u64 ev2 = 0, dtm = ~0ull;
-    f64 v2  = 0;
+    float v2 = 0.f;
     if (t < rs.n) {
         u32 a  = rs.row_rank[t];
         u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
@@ -403,21 +439,26 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
         lf.vy[iv] = nvy;
         lf.vz[iv] = nvz;
         lf.u[i]   = lf.u[i] + hdt * (tdu - odu);
-        ev2       = f64_to_ordered(ix * ix + iy * iy + iz * iz);
-        v2        = nvx * nvx + nvy * nvy + nvz * nvz;
-        f64 h_a   = h_rank[a];
-        f64 dt    = fmin(__longlong_as_double(0x7ff0000000000000ll), C_cour * h_a / (f64) vm);
-        f64 abs_a = sqrt(fx * fx + fy * fy + fz * fz);
-        dt        = fmin(dt, C_force * sqrt(h_a / abs_a));
-        dtm       = f64_to_ordered(dt);
+        // the rerun test, the mean |v|^2 and the CFL step only need FP32 (they feed a
+        // 1e-2 threshold, a normalisation and a time step)
+        const float fix = (float) ix, fiy = (float) iy, fiz = (float) iz;
+        ev2 = f64_to_ordered((f64) (fix * fix + fiy * fiy + fiz * fiz));
+        const float fvx = (float) nvx, fvy = (float) nvy, fvz = (float) nvz;
+        v2 = fvx * fvx + fvy * fvy + fvz * fvz;
+        const float hf  = (float) h_rank[a];
+        const float ffx = (float) fx, ffy = (float) fy, ffz = (float) fz;
+        const float abs_a = sqrtf(ffx * ffx + ffy * ffy + ffz * ffz);
+        float dt = fminf(__int_as_float(0x7f800000), (float) C_cour * hf / vm);
+        dt       = fminf(dt, (float) C_force * sqrtf(hf / abs_a));
+        dtm      = f64_to_ordered((f64) dt);
     }
     ev2 = block_reduce(ev2, OpMaxU64{}, 0ull);
     dtm = block_reduce(dtm, OpMinU64{}, ~0ull);
-    v2  = block_reduce(v2, OpAddF64{}, 0.0);
+    v2  = block_reduce(v2, OpAddF32{}, 0.f);
     if (threadIdx.x == 0) {
         atomicMax((unsigned long long *) &sc->epsv2_max, (unsigned long long) ev2);
         atomicMin((unsigned long long *) &sc->dt_min, (unsigned long long) dtm);
-        atomicAdd(&sc->sum_v2, v2);
+        atomicAdd(&sc->sum_v2, (f64) v2);
     }
 }
 
@@ -470,8 +511,9 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
 
 cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
                                const f64 *omega_local, f64 pmass, const EosParams &eos) {
-    StageEos se{eos.kind, eos.gamma, (float) (eos.gamma * (eos.gamma - 1)),
-                1.0 / (eos.r0 * eos.r0), (float) (eos.cs0 * eos.cs0), (float) -eos.q};
+    StageEos se{eos.kind, eos.gamma - 1, pmass * kHfact * kHfact * kHfact,
+                (float) (eos.gamma * (eos.gamma - 1)), (float) (1.0 / (eos.r0 * eos.r0)),
+                (float) (eos.cs0 * eos.cs0), (float) -eos.q};
     ProfScope ps(c, kProfGatherEos, N);
     { k_gather_stage_mixed<<<div_up(N, 256), 256, 0, c.stream>>>(
         c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf, omega_local, pmass, se,
