@@ -719,7 +719,10 @@ inline f64 inv_sat_zero(f64 v) { return (v != 0 && v == v) ? 1. / v : 0.; }
 void derivs_constAV(
     u32 n_local, const u32 *cnt, const u32 *scanned, const u32 *entries, const f64 *xyz,
     const f64 *vxyz, const f64 *hpart, const f64 *omega, const f64 *u, const f64 *pressure,
-    const f64 *cs, f64 pmass, f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *axyz, f64 *du) {
+    const f64 *cs, f64 pmass, f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *axyz, f64 *du,
+    const f64 *alpha = nullptr) {
+    // alpha (merged index space) != null: the varying-AV form, alpha_a and alpha_b per
+    // particle (NodeUpdateDerivsVaryingAlphaAV.cpp:45-125), otherwise alpha_AV for both
     const f64 Rker2 = Rkern * Rkern;
 #pragma omp parallel for schedule(dynamic, 1024)
     for (i64 ii = 0; ii < (i64) n_local; ii++) {
@@ -733,6 +736,7 @@ void derivs_constAV(
         f64 rho_a_inv         = 1. / rho_a;
         f64 omega_a_rho_a_inv = 1 / (omega_a * rho_a);
         f64 cs_a              = cs[a];
+        const f64 alpha_a     = alpha ? alpha[a] : alpha_AV;
         f64 fx = 0, fy = 0, fz = 0, tdu = 0;
         for (u32 k = scanned[a]; k < scanned[a] + cnt[a]; k++) {
             u32 b    = entries[k];
@@ -754,8 +758,9 @@ void derivs_constAV(
             f64 rx = dx * inv, ry = dy * inv, rz = dz * inv;
             f64 v_ab_r_ab     = vx * rx + vy * ry + vz * rz;
             f64 abs_v_ab_r_ab = std::fabs(v_ab_r_ab);
-            f64 vsig_a = alpha_AV * cs_a + beta_AV * abs_v_ab_r_ab;
-            f64 vsig_b = alpha_AV * cs_b + beta_AV * abs_v_ab_r_ab;
+            const f64 alpha_b = alpha ? alpha[b] : alpha_AV;
+            f64 vsig_a = alpha_a * cs_a + beta_AV * abs_v_ab_r_ab;
+            f64 vsig_b = alpha_b * cs_b + beta_AV * abs_v_ab_r_ab;
             // vsig_u (forces.hpp:35-41)
             f64 rho_avg = (rho_a + rho_b) * 0.5;
             f64 abs_dp  = std::fabs(P_a - P_b);
@@ -786,6 +791,121 @@ void derivs_constAV(
         axyz[3 * a + 1] = fy;
         axyz[3 * a + 2] = fz;
         du[a]           = tdu;
+    }
+}
+
+// Velocity-gradient estimates of the varying (CD10) viscosity, per local particle a over
+// its cache row, pairs inside max(h_a, h_b) R and grad W taken with h_a:
+//  - div v, curl v: -1/(Omega_a rho_a) sum m (v_a - v_b) . / x grad W
+//    (shammodels/sph/src/modules/DiffOperator.cpp:95-140, 200-245);
+//  - d(div v)/dt = tr(G(a)) - tr(G(v) G(v)) with the linearly corrected gradients
+//    G(f) = R^-1 D(f), R_ij = -sum m r_ab,i gradW_j, D(f)_jk = -sum m f_ab,k gradW_j
+//    (DiffOperatorDtDivv.cpp:116-210, 3x3 inverse by cofactors, matrix_legacy.hpp:25-95).
+// The three share one pass over the row; each sum keeps the reference's order.
+inline void inv33(const f64 m[3][3], f64 r[3][3]) {
+    const f64 a00 = m[0][0], a01 = m[0][1], a02 = m[0][2];
+    const f64 a10 = m[1][0], a11 = m[1][1], a12 = m[1][2];
+    const f64 a20 = m[2][0], a21 = m[2][1], a22 = m[2][2];
+    const f64 det = (((((-a02 * a11) * a20 + (a01 * a12) * a20) + (a02 * a10) * a21)
+                      - (a00 * a12) * a21) - (a01 * a10) * a22) + (a00 * a11) * a22;
+    r[0][0] = (-a12 * a21 + a11 * a22) / det;
+    r[0][1] = (a02 * a21 - a01 * a22) / det;
+    r[0][2] = (-a02 * a11 + a01 * a12) / det;
+    r[1][0] = (a12 * a20 - a10 * a22) / det;
+    r[1][1] = (-a02 * a20 + a00 * a22) / det;
+    r[1][2] = (a02 * a10 - a00 * a12) / det;
+    r[2][0] = (-a11 * a20 + a10 * a21) / det;
+    r[2][1] = (a01 * a20 - a00 * a21) / det;
+    r[2][2] = (-a01 * a10 + a00 * a11) / det;
+}
+inline void mul33(const f64 a[3][3], const f64 b[3][3], f64 c[3][3]) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) c[i][j] = (a[i][0] * b[0][j] + a[i][1] * b[1][j]) + a[i][2] * b[2][j];
+}
+
+void velocity_gradients(
+    u32 n_local, const u32 *cnt, const u32 *scanned, const u32 *entries, const f64 *xyz,
+    const f64 *vxyz, const f64 *axyz, const f64 *hpart, const f64 *omega, f64 pmass, f64 *divv,
+    f64 *curlv, f64 *dtdivv) {
+    const f64 Rker2 = Rkern * Rkern;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (i64 ii = 0; ii < (i64) n_local; ii++) {
+        u32 a = (u32) ii;
+        const f64 h_a = hpart[a];
+        const f64 *xa = &xyz[3 * a], *va = &vxyz[3 * a], *aa = &axyz[3 * a];
+        const f64 rho_a = rho_h(pmass, h_a, hfactd);
+        const f64 inv_rho_omega_a = 1. / (omega[a] * rho_a);
+        f64 sdiv = 0, sc[3] = {0, 0, 0};
+        f64 R[3][3] = {}, Dv[3][3] = {}, Da[3][3] = {};
+        for (u32 k = scanned[a]; k < scanned[a] + cnt[a]; k++) {
+            u32 b = entries[k];
+            const f64 r[3] = {xa[0] - xyz[3 * b], xa[1] - xyz[3 * b + 1], xa[2] - xyz[3 * b + 2]};
+            const f64 rab2 = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
+            const f64 h_b  = hpart[b];
+            if (rab2 > h_a * h_a * Rker2 && rab2 > h_b * h_b * Rker2) continue;
+            const f64 rab = std::sqrt(rab2);
+            const f64 v[3] = {va[0] - vxyz[3 * b], va[1] - vxyz[3 * b + 1], va[2] - vxyz[3 * b + 2]};
+            const f64 w[3] = {aa[0] - axyz[3 * b], aa[1] - axyz[3 * b + 1], aa[2] - axyz[3 * b + 2]};
+            f64 e[3] = {r[0] / rab, r[1] / rab, r[2] / rab};
+            if (rab < 1e-9) e[0] = e[1] = e[2] = 0;
+            const f64 F = dW_3d(rab, h_a);
+            const f64 g[3] = {F * e[0], F * e[1], F * e[2]};
+            sdiv = sdiv + pmass * ((v[0] * g[0] + v[1] * g[1]) + v[2] * g[2]);
+            sc[0] = sc[0] + pmass * (v[1] * g[2] - v[2] * g[1]);
+            sc[1] = sc[1] + pmass * (v[2] * g[0] - v[0] * g[2]);
+            sc[2] = sc[2] + pmass * (v[0] * g[1] - v[1] * g[0]);
+            const f64 mg[3] = {g[0] * pmass, g[1] * pmass, g[2] * pmass};
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    R[i][j]  = R[i][j] - r[i] * mg[j];
+                    Dv[j][i] = Dv[j][i] - v[i] * mg[j];
+                    Da[j][i] = Da[j][i] - w[i] * mg[j];
+                }
+        }
+        divv[a] = -inv_rho_omega_a * sdiv;
+        for (int c = 0; c < 3; c++) curlv[3 * a + c] = -inv_rho_omega_a * sc[c];
+        f64 Ri[3][3], Gv[3][3], Ga[3][3];
+        inv33(R, Ri);
+        mul33(Ri, Dv, Gv);
+        mul33(Ri, Da, Ga);
+        const f64 div_a = (Ga[0][0] + Ga[1][1]) + Ga[2][2];
+        const f64 tens  = ((((((((Gv[0][0] * Gv[0][0] + Gv[1][0] * Gv[0][1]) + Gv[2][0] * Gv[0][2])
+                                + Gv[0][1] * Gv[1][0]) + Gv[1][1] * Gv[1][1]) + Gv[2][1] * Gv[1][2])
+                             + Gv[0][2] * Gv[2][0]) + Gv[1][2] * Gv[2][1]) + Gv[2][2] * Gv[2][2]);
+        dtdivv[a] = div_a - tens;
+    }
+}
+
+// Cullen & Dehnen (2010) viscosity switch, one implicit-Euler relaxation step
+// (shammodels/sph/src/modules/UpdateViscosity.cpp:170-215); cs is the sound speed kept
+// from the previous step's last EOS evaluation.
+void cd10_update(u32 n, const f64 *divv, const f64 *curlv, const f64 *dtdivv, const f64 *cs,
+                 const f64 *h, const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min,
+                 f64 alpha_max, f64 *alpha_new) {
+    const f64 eps = std::numeric_limits<f64>::epsilon();
+#pragma omp parallel for schedule(static)
+    for (i64 ii = 0; ii < (i64) n; ii++) {
+        const u32 i = (u32) ii;
+        const f64 cs_a = cs[i], h_a = h[i], alpha_a = alpha[i];
+        const f64 inv_tau = cs_a * sigma_decay / h_a;
+        const f64 fact_t  = dt * inv_tau;
+        const f64 euler   = 1 / (1 + fact_t);
+        // max / min written as comparisons (NaN and signed-zero cases fixed, as on the GPU)
+        const f64 md = -divv[i];
+        f64 fac      = (md > 0) ? md : f64(0);
+        fac          = fac * fac;
+        const f64 traceS = (curlv[3 * i] * curlv[3 * i] + curlv[3 * i + 1] * curlv[3 * i + 1])
+                           + curlv[3 * i + 2] * curlv[3 * i + 2];
+        const f64 balsara = (fac + traceS > eps) ? fac / (fac + traceS) : f64(1);
+        const f64 mdt     = -dtdivv[i];
+        const f64 A       = balsara * ((mdt > 0) ? mdt : f64(0));
+        const f64 temp    = cs_a * cs_a;
+        f64 alpha_loc     = (cs_a > 0) ? 10 * h_a * h_a * A / temp : alpha_min;
+        alpha_loc         = (alpha_loc < alpha_max) ? alpha_loc : alpha_max;
+        alpha_loc     = (temp > eps) ? alpha_loc : alpha_min;
+        f64 na = (alpha_a + alpha_loc * fact_t) * euler;
+        if (alpha_loc > alpha_a) na = alpha_loc;
+        alpha_new[i] = na;
     }
 }
 
@@ -964,6 +1084,9 @@ struct Config {
     u32 ext_kind; // 0 none, 1 central point mass
     f64 cs0, eos_r0, eos_q;        // LP07: c_s^2 = cs0^2 (R^2 / r0^2)^(-q)
     f64 central_mass, constant_G;  // point mass at the origin
+    u32 av_kind;  // 0 constant, 1 varying CD10 (Cullen & Dehnen 2010)
+    u32 pad;
+    f64 alpha_min, alpha_max, sigma_decay;
 };
 
 struct StepLog {
@@ -984,6 +1107,8 @@ struct Sim {
     Tree tree;
     NeighCache cache;
     std::vector<f64> P, cs, vsig;
+    // varying AV state (alpha_AV, the sound speed of the last EOS) and its diagnostics
+    std::vector<f64> alpha_AV, soundspeed, divv, curlv, dtdivv;
 };
 
 void merge_positions(Sim &s, std::vector<f64> &mxyz, std::vector<f64> &mh) {
@@ -1092,6 +1217,26 @@ void evolve_once(Sim &s, StepLog &log) {
         merge_field(s, s.vxyz, 3, m_v);
         merge_field(s, s.omega, 1, m_om);
         u32 N = (u32) m_h.size();
+        // varying AV (Solver.cpp:2261-2370): div v, curl v, d(div v)/dt with the current
+        // velocities and the accelerations of the last evaluation, the switch update from
+        // alpha_AV, then alpha on the ghosts
+        std::vector<f64> alpha_upd, m_alpha;
+        if (cfg.av_kind == 1) {
+            std::vector<f64> m_a;
+            merge_field(s, s.axyz, 3, m_a);
+            s.divv.assign(n, 0);
+            s.curlv.assign(3 * (size_t) n, 0);
+            s.dtdivv.assign(n, 0);
+            velocity_gradients(n, s.cache.part.cnt.data(), s.cache.part.scanned.data(),
+                               s.cache.part.entries.data(), mxyz.data(), m_v.data(), m_a.data(),
+                               m_h.data(), m_om.data(), cfg.pmass, s.divv.data(), s.curlv.data(),
+                               s.dtdivv.data());
+            alpha_upd.assign(n, 0);
+            cd10_update(n, s.divv.data(), s.curlv.data(), s.dtdivv.data(), s.soundspeed.data(),
+                        s.h.data(), s.alpha_AV.data(), dt, cfg.sigma_decay, cfg.alpha_min,
+                        cfg.alpha_max, alpha_upd.data());
+            merge_field(s, alpha_upd, 1, m_alpha);
+        }
         s.P.assign(N, 0);
         s.cs.assign(N, 0);
         if (cfg.eos_kind == 1)
@@ -1103,7 +1248,8 @@ void evolve_once(Sim &s, StepLog &log) {
         derivs_constAV(n, s.cache.part.cnt.data(), s.cache.part.scanned.data(),
                        s.cache.part.entries.data(), mxyz.data(), m_v.data(), m_h.data(),
                        m_om.data(), m_u.data(), s.P.data(), s.cs.data(), cfg.pmass, cfg.alpha_u,
-                       cfg.alpha_AV, cfg.beta_AV, s.axyz.data(), s.du.data());
+                       cfg.alpha_AV, cfg.beta_AV, s.axyz.data(), s.du.data(),
+                       cfg.av_kind == 1 ? m_alpha.data() : nullptr);
         if (cfg.ext_kind == 1)
             for (size_t k = 0; k < 3 * (size_t) n; k++) s.axyz[k] = s.axyz[k] + aext[k];
         f64 eps_v = leapfrog_correct(n, s.vxyz.data(), s.u.data(), s.axyz.data(), old_a.data(),
@@ -1114,6 +1260,11 @@ void evolve_once(Sim &s, StepLog &log) {
             s.cfl_mult = s.cfl_mult / 2;
         } else {
             rerun = false;
+            if (cfg.av_kind == 1) {
+                // write back (Solver.cpp:2620-2650, 3125-3160)
+                s.alpha_AV = alpha_upd;
+                s.soundspeed.assign(s.cs.begin(), s.cs.begin() + n);
+            }
             s.vsig.assign(n, 0);
             vsig_max(n, s.cache.part.cnt.data(), s.cache.part.scanned.data(),
                      s.cache.part.entries.data(), mxyz.data(), m_v.data(), m_h.data(), s.cs.data(),
@@ -1337,7 +1488,25 @@ void *orc_sim_create(const orc::Config *cfg, u32 n, const f64 *xyz, const f64 *v
     s->axyz.assign(3 * (size_t) n, 0);
     s->du.assign(n, 0);
     s->omega.assign(n, 1);
+    s->alpha_AV.assign(n, cfg->alpha_AV);
+    s->soundspeed.assign(n, 0);
     return s;
+}
+// varying-AV state: alpha_AV and the stored sound speed (in and out), the last step's
+// div v, curl v (3 per particle), d(div v)/dt (out)
+void orc_sim_set_av(void *sp, const f64 *alpha, const f64 *cs) {
+    orc::Sim *s = (orc::Sim *) sp;
+    if (alpha) std::memcpy(s->alpha_AV.data(), alpha, 8 * (size_t) s->n);
+    if (cs) std::memcpy(s->soundspeed.data(), cs, 8 * (size_t) s->n);
+}
+void orc_sim_get_av(void *sp, f64 *alpha, f64 *cs, f64 *divv, f64 *curlv, f64 *dtdivv) {
+    orc::Sim *s = (orc::Sim *) sp;
+    u32 n       = s->n;
+    if (alpha) std::memcpy(alpha, s->alpha_AV.data(), 8 * (size_t) n);
+    if (cs) std::memcpy(cs, s->soundspeed.data(), 8 * (size_t) n);
+    if (divv && s->divv.size() == n) std::memcpy(divv, s->divv.data(), 8 * (size_t) n);
+    if (curlv && s->curlv.size() == 3 * (size_t) n) std::memcpy(curlv, s->curlv.data(), 24 * (size_t) n);
+    if (dtdivv && s->dtdivv.size() == n) std::memcpy(dtdivv, s->dtdivv.data(), 8 * (size_t) n);
 }
 void orc_sim_free(void *s) { delete (orc::Sim *) s; }
 void orc_sim_set_time(void *sp, f64 t, f64 dt, f64 cfl_mult) {

@@ -36,6 +36,8 @@ class OrcConfig(C.Structure):
         ("eos_kind", C.c_uint32), ("ext_kind", C.c_uint32),
         ("cs0", C.c_double), ("eos_r0", C.c_double), ("eos_q", C.c_double),
         ("central_mass", C.c_double), ("constant_G", C.c_double),
+        ("av_kind", C.c_uint32), ("pad", C.c_uint32),
+        ("alpha_min", C.c_double), ("alpha_max", C.c_double), ("sigma_decay", C.c_double),
     ]
 
 
@@ -119,6 +121,8 @@ def lib():
         "orc_sim_set_derivs": (None, [_vp, _f64p, _f64p]),
         "orc_sim_evolve_once": (None, [_vp, C.POINTER(OrcStepLog)]),
         "orc_sim_get": (None, [_vp] + [_vp] * 7),
+        "orc_sim_set_av": (None, [_vp, _vp, _vp]),
+        "orc_sim_get_av": (None, [_vp] + [_vp] * 5),
         "orc_sim_ghost_count": (C.c_uint32, [_vp]),
         "orc_sim_ghosts": (None, [_vp, _u32p, _f64p]),
         "orc_sim_cache": (_vp, [_vp]),
@@ -366,6 +370,22 @@ class Sim:
                  axyz=np.zeros((n, 3)), duint=np.zeros(n), omega=np.zeros(n))
         lib().orc_sim_get(self.handle, *[_ptr(d[k]) for k in (
             "xyz", "vxyz", "hpart", "uint", "axyz", "duint", "omega")])
+        return d
+
+    def set_av(self, alpha=None, soundspeed=None):
+        """Varying-AV state: per-particle alpha_AV and the stored sound speed."""
+        a = None if alpha is None else _f64(alpha)
+        c = None if soundspeed is None else _f64(soundspeed)
+        lib().orc_sim_set_av(self.handle, None if a is None else _ptr(a),
+                             None if c is None else _ptr(c))
+
+    def get_av(self):
+        """alpha_AV, soundspeed, and the last step's divv, curlv (n, 3), dtdivv."""
+        n = self.n
+        d = dict(alpha_AV=np.zeros(n), soundspeed=np.zeros(n), divv=np.zeros(n),
+                 curlv=np.zeros((n, 3)), dtdivv=np.zeros(n))
+        lib().orc_sim_get_av(self.handle, *[_ptr(d[k]) for k in (
+            "alpha_AV", "soundspeed", "divv", "curlv", "dtdivv")])
         return d
 
     def ghosts(self):
