@@ -58,6 +58,15 @@ typedef struct {
     gbsph_vec3 xyz, vxyz, axyz;
     double *hpart, *uint, *duint;
     double *omega; /* optional output, may be NULL */
+    /* Varying viscosity (av_kind GBSPH_AV_VARYING_CD10) only, NULL otherwise.  State
+     * carried between steps, read and updated in place: alpha_AV and soundspeed (the
+     * sound speed of the last EOS evaluation, the reference's "soundspeed" field;
+     * zero-initialised like the reference's fields).  Optional outputs of the last
+     * corrector evaluation: divv, curlv, dtdivv (the reference's fields of those names). */
+    double *alpha_AV, *soundspeed;
+    double *divv;
+    gbsph_vec3 curlv;
+    double *dtdivv;
 } gbsph_particles;
 
 /* Solver configuration (the hot-path subset of shammodels::sph::SolverConfig,
@@ -92,12 +101,22 @@ typedef struct {
     uint32_t ext_kind;
     double cs0, eos_r0, eos_q;
     double central_mass, constant_G;
+    /* Artificial viscosity: GBSPH_AV_CONSTANT (alpha_AV) or GBSPH_AV_VARYING_CD10,
+     * Cullen & Dehnen (2010): per-particle alpha relaxed towards a shock indicator built
+     * from div v, curl v and d(div v)/dt, in [alpha_min, alpha_max] with decay rate
+     * sigma_decay (AVConfig::VaryingCD10, UpdateViscosity.cpp:122-215); alpha_u and
+     * beta_AV as for the constant form. */
+    uint32_t av_kind;
+    uint32_t pad2;
+    double alpha_min, alpha_max, sigma_decay;
 } gbsph_config;
 
 #define GBSPH_EOS_ADIABATIC 0
 #define GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07 1
 #define GBSPH_EXT_NONE 0
 #define GBSPH_EXT_POINT_MASS 1
+#define GBSPH_AV_CONSTANT 0
+#define GBSPH_AV_VARYING_CD10 1
 
 /* Synchronised solver state (the scheduler edges "time", "dt", "cfl_multiplier",
  * shammodels/sph/include/shammodels/sph/Solver.hpp:99-145). */

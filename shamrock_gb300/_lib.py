@@ -18,6 +18,8 @@ GBSPH_ERR_NOT_CONVERGED = 4
 GBSPH_ERR_STATE = 5
 GBSPH_FP64 = 0
 GBSPH_MIXED = 1
+GBSPH_AV_CONSTANT = 0
+GBSPH_AV_VARYING_CD10 = 1
 
 _vp = C.c_void_p
 _u32 = C.c_uint32
@@ -32,7 +34,9 @@ class Vec3(C.Structure):
 
 class Particles(C.Structure):
     _fields_ = [("n", _u32), ("pad", _u32), ("xyz", Vec3), ("vxyz", Vec3), ("axyz", Vec3),
-                ("hpart", _vp), ("uint", _vp), ("duint", _vp), ("omega", _vp)]
+                ("hpart", _vp), ("uint", _vp), ("duint", _vp), ("omega", _vp),
+                ("alpha_AV", _vp), ("soundspeed", _vp), ("divv", _vp), ("curlv", Vec3),
+                ("dtdivv", _vp)]
 
 
 class Config(C.Structure):
@@ -44,7 +48,8 @@ class Config(C.Structure):
                 ("box_max", _d3), ("precision", _u32), ("pad", _u32),
                 ("epsilon_h_particle", _f64), ("eos_kind", _u32), ("ext_kind", _u32),
                 ("cs0", _f64), ("eos_r0", _f64), ("eos_q", _f64), ("central_mass", _f64),
-                ("constant_G", _f64)]
+                ("constant_G", _f64), ("av_kind", _u32), ("pad2", _u32), ("alpha_min", _f64),
+                ("alpha_max", _f64), ("sigma_decay", _f64)]
 
 
 class TimeState(C.Structure):

@@ -64,7 +64,8 @@ Ctx::~Ctx() {
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
                       &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
-                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &aext};
+                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &aext, &av_arank,
+                      &av_alpha_rank, &av_alpha_upd, &av_diag};
     cudaSetDevice(device);
     for (DevBuf *b : bufs) b->release(stream);
     cudaStreamSynchronize(stream);
@@ -195,7 +196,7 @@ const char *gbsph_version(void) { return "gbsph 0.1 (sm_103a)"; }
 static const char *kProfNames[kProfCount] = {
     "predict", "ghosts", "merge_bbox", "morton_sort", "tree", "leaf_lists", "owner",
     "cache_count", "cache_fill", "h_iterate", "omega", "gather_eos", "derivs", "adj_derivs",
-    "adj_density"};
+    "adj_density", "velgrad"};
 
 uint32_t gbsph_profile_kinds(void) { return kProfCount; }
 
@@ -586,6 +587,14 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
                 "unknown external force");
     REQUIRE_ARG(cfg->eos_kind != GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07 || cfg->eos_r0 > 0,
                 "locally isothermal EOS needs r0 > 0");
+    REQUIRE_ARG(cfg->av_kind == GBSPH_AV_CONSTANT || cfg->av_kind == GBSPH_AV_VARYING_CD10,
+                "unknown artificial viscosity");
+    const bool cd10 = cfg->av_kind == GBSPH_AV_VARYING_CD10;
+    REQUIRE_ARG(!cd10 || (p->alpha_AV && p->soundspeed),
+                "the varying viscosity needs the alpha_AV and soundspeed fields");
+    REQUIRE_ARG(!cd10 || !tape, "the adjoint step supports the constant viscosity only");
+    REQUIRE_ARG(!cd10 || !p->curlv.x || (p->curlv.y && p->curlv.z && p->curlv.stride > 0),
+                "curlv needs its three components and a stride");
     auto t_start = std::chrono::steady_clock::now();
     cudaStream_t s = c.stream;
     const u32 n    = p->n;
@@ -725,8 +734,50 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             return fail(ctx, GBSPH_ERR_NOT_CONVERGED,
                         "the corrector has made over 50 loops, either their is a bug, either you "
                         "are using a dt that is too large");
-        if (mixed) CU(gather_stage_mixed(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
+        if (mixed) CU(gather_stage_mixed(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos, cd10));
         else CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
+        hs.alpha = nullptr;
+        if (cd10) {
+            // varying viscosity (Solver.cpp:2261-2370): div v, curl v and d(div v)/dt from
+            // the current velocities and the accelerations of the last evaluation, the
+            // switch update from alpha_AV and the stored sound speed, alpha on the ghosts.
+            // (EOS values do not enter these, so staging them first changes nothing.)
+            CU(c.av_diag.ensure(sizeof(f64) * 5 * (size_t) n, s));
+            CU(c.av_alpha_upd.ensure(sizeof(f64) * (size_t) n, s));
+            f64 *diag = c.av_diag.as<f64>();
+            f64 *divv = p->divv ? p->divv : diag;
+            f64 *dtdv = p->dtdivv ? p->dtdivv : diag + n;
+            f64 *cx = p->curlv.x, *cy = p->curlv.y, *cz = p->curlv.z;
+            u32 cvs = p->curlv.stride;
+            if (!cx) {
+                cx  = diag + 2 * (size_t) n;
+                cy  = diag + 3 * (size_t) n;
+                cz  = diag + 4 * (size_t) n;
+                cvs = 1;
+            }
+            f64 *alpha_upd = c.av_alpha_upd.as<f64>();
+            if (mixed) {
+                CU(velgrad_mixed(c, rs, c.omega_local.as<f64>(), cfg->pmass, divv, cx, cy, cz, cvs,
+                                 dtdv));
+            } else {
+                CU(c.av_arank.ensure(sizeof(f64) * 3 * (size_t) N, s));
+                f64 *ar = c.av_arank.as<f64>();
+                CU(gather_merged64(c, N, n, lf.ax, lf.vs, ar));
+                CU(gather_merged64(c, N, n, lf.ay, lf.vs, ar + N));
+                CU(gather_merged64(c, N, n, lf.az, lf.vs, ar + 2 * (size_t) N));
+                CU(velgrad64(c, rs, hs, ar, ar + N, ar + 2 * (size_t) N, cfg->pmass, divv, cx, cy,
+                             cz, cvs, dtdv));
+            }
+            CU(cd10_update(c, n, divv, cx, cy, cz, cvs, dtdv, p->soundspeed, lf.h, p->alpha_AV,
+                           dt, cfg->sigma_decay, cfg->alpha_min, cfg->alpha_max, alpha_upd));
+            if (mixed) {
+                CU(stage_alpha_mixed(c, N, n, alpha_upd));
+            } else {
+                CU(c.av_alpha_rank.ensure(sizeof(f64) * (size_t) N, s));
+                CU(gather_merged64(c, N, n, alpha_upd, 1, c.av_alpha_rank.as<f64>()));
+                hs.alpha = c.av_alpha_rank.as<f64>();
+            }
+        }
         if (tape) {
             { k_snap_vu<<<div_up(n, 256), 256, 0, s>>>(
                 n, lf.vx, lf.vy, lf.vz, lf.vs, lf.u,
@@ -738,7 +789,7 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
         if (mixed)
             CU(derivs_step_mixed(c, rs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
-                                 dt / 2, C_cour, C_force, lf, ext));
+                                 dt / 2, C_cour, C_force, lf, ext, cd10));
         else
             CU(derivs_step64(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
                              dt / 2, C_cour, C_force, lf, ext));
@@ -757,6 +808,14 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         } else {
             rerun    = false;
             next_cfl = ordered_to_f64(c.h_scalars->dt_min);
+        }
+        if (cd10 && !rerun) {
+            // write back alpha_AV and the sound speed of this evaluation
+            // (Solver.cpp:2620-2650, 3125-3160)
+            CU(cudaMemcpyAsync(p->alpha_AV, c.av_alpha_upd.p, sizeof(f64) * (size_t) n,
+                               cudaMemcpyDeviceToDevice, s));
+            if (mixed) CU(cs_to_local_mixed(c, n, p->soundspeed));
+            else CU(rank_to_local64(c, n, c.scs.as<f64>(), p->soundspeed));
         }
         corr_iters++;
     } while (rerun);

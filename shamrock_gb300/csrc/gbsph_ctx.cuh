@@ -81,6 +81,7 @@ enum ProfKind : int {
     kProfDerivs,
     kProfAdjDerivs, // adjoint: reverse of the derivatives (staging + pair kernel)
     kProfAdjDensity, // adjoint: reverse of Omega and the density constraint
+    kProfVelGrad,    // varying AV: div v, curl v, d(div v)/dt and the switch
     kProfCount
 };
 
@@ -146,6 +147,9 @@ struct Ctx {
     // ---- per-row / per-local work arrays
     DevBuf h_old_row, eps_row, omega_local, a_old, du_old, hnew_row, omega_row;
     DevBuf aext; // external acceleration of the step (3 n, SoA)
+    // varying AV: rank-ordered accelerations (3 N) and alpha (N), the updated alpha (n),
+    // div v / curl v / d(div v)/dt when the caller does not take them (5 n)
+    DevBuf av_arank, av_alpha_rank, av_alpha_upd, av_diag;
     DevBuf dt_part;
 
     // ---- adjoint: working state, tape, accumulators (local and rank order)

@@ -223,6 +223,7 @@ __device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace 
     f64 rho_a_inv         = 1. / rho_a;
     f64 omega_a_rho_a_inv = 1 / (omega_a * rho_a);
     f64 cs_a              = hs.cs[a];
+    const f64 alpha_a     = hs.alpha ? hs.alpha[a] : p.alpha_AV;
     fx = fy = fz = tdu = 0;
     vsig_max           = 0;
     for (u32 k = k0; k < k1; k++) {
@@ -244,8 +245,10 @@ __device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace 
         f64 rx = dx * inv, ry = dy * inv, rz = dz * inv;
         f64 v_ab_r_ab     = vx * rx + vy * ry + vz * rz;
         f64 abs_v_ab_r_ab = fabs(v_ab_r_ab);
-        f64 vsig_a  = p.alpha_AV * cs_a + p.beta_AV * abs_v_ab_r_ab;
-        f64 vsig_b  = p.alpha_AV * cs_b + p.beta_AV * abs_v_ab_r_ab;
+        // varying AV: alpha_a, alpha_b per particle (NodeUpdateDerivsVaryingAlphaAV.cpp:95-96)
+        const f64 alpha_b = hs.alpha ? hs.alpha[b] : p.alpha_AV;
+        f64 vsig_a  = alpha_a * cs_a + p.beta_AV * abs_v_ab_r_ab;
+        f64 vsig_b  = alpha_b * cs_b + p.beta_AV * abs_v_ab_r_ab;
         f64 rho_avg = (rho_a + rho_b) * 0.5;
         f64 abs_dp  = fabs(P_a - P_b);
         f64 vsig_u  = sqrt(abs_dp / rho_avg);
@@ -407,6 +410,145 @@ __global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f
     lf.u[i]   = u;
 }
 
+// ---------------------------------------------------------------- varying AV (CD10)
+// div v and curl v (DiffOperator.cpp:95-140, 200-245) and d(div v)/dt from the linearly
+// corrected gradients (DiffOperatorDtDivv.cpp:116-210) in one pass over the row; each
+// sum in the reference's order, so the values equal the three separate kernels'.
+__device__ __forceinline__ void inv33(const f64 m[3][3], f64 r[3][3]) {
+    const f64 a00 = m[0][0], a01 = m[0][1], a02 = m[0][2];
+    const f64 a10 = m[1][0], a11 = m[1][1], a12 = m[1][2];
+    const f64 a20 = m[2][0], a21 = m[2][1], a22 = m[2][2];
+    const f64 det = (((((-a02 * a11) * a20 + (a01 * a12) * a20) + (a02 * a10) * a21)
+                      - (a00 * a12) * a21) - (a01 * a10) * a22) + (a00 * a11) * a22;
+    r[0][0] = (-a12 * a21 + a11 * a22) / det;
+    r[0][1] = (a02 * a21 - a01 * a22) / det;
+    r[0][2] = (-a02 * a11 + a01 * a12) / det;
+    r[1][0] = (a12 * a20 - a10 * a22) / det;
+    r[1][1] = (-a02 * a20 + a00 * a22) / det;
+    r[1][2] = (a02 * a10 - a00 * a12) / det;
+    r[2][0] = (-a11 * a20 + a10 * a21) / det;
+    r[2][1] = (a01 * a20 - a00 * a21) / det;
+    r[2][2] = (-a01 * a10 + a00 * a11) / det;
+}
+__device__ __forceinline__ void mul33(const f64 a[3][3], const f64 b[3][3], f64 c[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) c[i][j] = (a[i][0] * b[0][j] + a[i][1] * b[1][j]) + a[i][2] * b[2][j];
+}
+
+__global__ void __launch_bounds__(128) k_velgrad64(RowSpace rs, HydroSpace hs,
+                                                   const f64 *__restrict__ axr,
+                                                   const f64 *__restrict__ ayr,
+                                                   const f64 *__restrict__ azr, f64 pmass,
+                                                   f64 *__restrict__ divv, f64 *__restrict__ cx,
+                                                   f64 *__restrict__ cy, f64 *__restrict__ cz,
+                                                   u32 cvs, f64 *__restrict__ dtdivv) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    const u32 a  = rs.row_rank[t];
+    const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    const f64 Rker2 = kRkern * kRkern;
+    const f64 h_a   = hs.h[a];
+    const f64 xa[3] = {rs.x[a], rs.y[a], rs.z[a]};
+    const f64 va[3] = {hs.vx[a], hs.vy[a], hs.vz[a]};
+    const f64 aa[3] = {axr[a], ayr[a], azr[a]};
+    const f64 rho_a = rho_h(pmass, h_a);
+    const f64 inv_rho_omega_a = 1. / (hs.omega[a] * rho_a);
+    f64 sdiv = 0, sc[3] = {0, 0, 0};
+    f64 R[3][3] = {}, Dv[3][3] = {}, Da[3][3] = {};
+    for (u32 k = k0; k < k1; k++) {
+        const u32 b    = rs.ent[k];
+        const f64 r[3] = {xa[0] - rs.x[b], xa[1] - rs.y[b], xa[2] - rs.z[b]};
+        const f64 rab2 = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
+        const f64 h_b  = hs.h[b];
+        if (rab2 > h_a * h_a * Rker2 && rab2 > h_b * h_b * Rker2) continue;
+        const f64 rab  = sqrt(rab2);
+        const f64 v[3] = {va[0] - hs.vx[b], va[1] - hs.vy[b], va[2] - hs.vz[b]};
+        const f64 w[3] = {aa[0] - axr[b], aa[1] - ayr[b], aa[2] - azr[b]};
+        f64 e[3] = {r[0] / rab, r[1] / rab, r[2] / rab};
+        if (rab < 1e-9) e[0] = e[1] = e[2] = 0;
+        const f64 F    = dW_3d(rab, h_a);
+        const f64 g[3] = {F * e[0], F * e[1], F * e[2]};
+        sdiv  = sdiv + pmass * ((v[0] * g[0] + v[1] * g[1]) + v[2] * g[2]);
+        sc[0] = sc[0] + pmass * (v[1] * g[2] - v[2] * g[1]);
+        sc[1] = sc[1] + pmass * (v[2] * g[0] - v[0] * g[2]);
+        sc[2] = sc[2] + pmass * (v[0] * g[1] - v[1] * g[0]);
+        const f64 mg[3] = {g[0] * pmass, g[1] * pmass, g[2] * pmass};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                R[i][j]  = R[i][j] - r[i] * mg[j];
+                Dv[j][i] = Dv[j][i] - v[i] * mg[j];
+                Da[j][i] = Da[j][i] - w[i] * mg[j];
+            }
+    }
+    const u32 i = rs.row_local[t];
+    divv[i]     = -inv_rho_omega_a * sdiv;
+    cx[(size_t) i * cvs] = -inv_rho_omega_a * sc[0];
+    cy[(size_t) i * cvs] = -inv_rho_omega_a * sc[1];
+    cz[(size_t) i * cvs] = -inv_rho_omega_a * sc[2];
+    f64 Ri[3][3], Gv[3][3], Ga[3][3];
+    inv33(R, Ri);
+    mul33(Ri, Dv, Gv);
+    mul33(Ri, Da, Ga);
+    const f64 div_a = (Ga[0][0] + Ga[1][1]) + Ga[2][2];
+    const f64 tens  = ((((((((Gv[0][0] * Gv[0][0] + Gv[1][0] * Gv[0][1]) + Gv[2][0] * Gv[0][2])
+                            + Gv[0][1] * Gv[1][0]) + Gv[1][1] * Gv[1][1]) + Gv[2][1] * Gv[1][2])
+                         + Gv[0][2] * Gv[2][0]) + Gv[1][2] * Gv[2][1]) + Gv[2][2] * Gv[2][2]);
+    dtdivv[i] = div_a - tens;
+}
+
+// Cullen & Dehnen (2010) switch, one implicit-Euler step (UpdateViscosity.cpp:170-215);
+// max / min as comparisons, as in the oracle
+__global__ void k_cd10(u32 n, const f64 *__restrict__ divv, const f64 *__restrict__ cx,
+                       const f64 *__restrict__ cy, const f64 *__restrict__ cz, u32 cvs,
+                       const f64 *__restrict__ dtdivv, const f64 *__restrict__ cs,
+                       const f64 *__restrict__ h, const f64 *__restrict__ alpha, f64 dt,
+                       f64 sigma_decay, f64 alpha_min, f64 alpha_max, f64 *__restrict__ alpha_new) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f64 eps  = 2.220446049250313e-16; // DBL_EPSILON
+    const f64 cs_a = cs[i], h_a = h[i], alpha_a = alpha[i];
+    const f64 inv_tau = cs_a * sigma_decay / h_a;
+    const f64 fact_t  = dt * inv_tau;
+    const f64 euler   = 1 / (1 + fact_t);
+    const f64 md = -divv[i];
+    f64 fac      = (md > 0) ? md : f64(0);
+    fac          = fac * fac;
+    const size_t iv  = (size_t) i * cvs;
+    const f64 traceS = (cx[iv] * cx[iv] + cy[iv] * cy[iv]) + cz[iv] * cz[iv];
+    const f64 balsara = (fac + traceS > eps) ? fac / (fac + traceS) : f64(1);
+    const f64 mdt     = -dtdivv[i];
+    const f64 A       = balsara * ((mdt > 0) ? mdt : f64(0));
+    const f64 temp    = cs_a * cs_a;
+    f64 alpha_loc     = (cs_a > 0) ? 10 * h_a * h_a * A / temp : alpha_min;
+    alpha_loc         = (alpha_loc < alpha_max) ? alpha_loc : alpha_max;
+    alpha_loc         = (temp > eps) ? alpha_loc : alpha_min;
+    f64 na = (alpha_a + alpha_loc * fact_t) * euler;
+    if (alpha_loc > alpha_a) na = alpha_loc;
+    alpha_new[i] = na;
+}
+
+__global__ void k_gather_merged(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
+                                const u32 *__restrict__ ghost_src, const f64 *__restrict__ src,
+                                u32 stride, f64 *__restrict__ dst) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    u32 id  = sort_index[r];
+    u32 s   = id < n_local ? id : ghost_src[id - n_local];
+    dst[r]  = src[(size_t) s * stride];
+}
+
+__global__ void k_rank_to_local(u32 n, const u32 *__restrict__ row_rank,
+                                const u32 *__restrict__ row_local, const f64 *__restrict__ src,
+                                f64 *__restrict__ dst) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    dst[row_local[t]] = src[row_rank[t]];
+}
+
 __global__ void k_scatter_rows(u32 n, const u32 *__restrict__ row_local, const f64 *__restrict__ src,
                                f64 *__restrict__ dst) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -546,6 +688,35 @@ cudaError_t predict64(Ctx &c, const LocalFields &lf, u32 n, f64 dt, int periodic
     { k_predict<<<div_up(n, 256), 256, 0, c.stream>>>(lf, n, dt, periodic, bmin[0], bmin[1], bmin[2],
                                                    bmax[0], bmax[1], bmax[2], mGM, ext_x, ext_y,
                                                    ext_z); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t velgrad64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, const f64 *ax,
+                      const f64 *ay, const f64 *az, f64 pmass, f64 *divv, f64 *cx, f64 *cy,
+                      f64 *cz, u32 cvs, f64 *dtdivv) {
+    ProfScope ps(c, kProfVelGrad, rs.n);
+    { k_velgrad64<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, ax, ay, az, pmass, divv, cx, cy,
+                                                         cz, cvs, dtdivv); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64 *cy,
+                        const f64 *cz, u32 cvs, const f64 *dtdivv, const f64 *cs, const f64 *h,
+                        const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
+                        f64 *alpha_new) {
+    { k_cd10<<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cx, cy, cz, cvs, dtdivv, cs, h, alpha,
+                                                  dt, sigma_decay, alpha_min, alpha_max,
+                                                  alpha_new); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t gather_merged64(Ctx &c, u32 N, u32 n_local, const f64 *src, u32 stride, f64 *dst) {
+    { k_gather_merged<<<div_up(N, 256), 256, 0, c.stream>>>(c.sort_index.as<u32>(), N, n_local,
+                                                           c.ghost_src.as<u32>(), src, stride,
+                                                           dst); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t rank_to_local64(Ctx &c, u32 n, const f64 *src_rank, f64 *dst) {
+    { k_rank_to_local<<<div_up(n, 256), 256, 0, c.stream>>>(n, c.row_rank.as<u32>(),
+                                                           c.row_local.as<u32>(), src_rank,
+                                                           dst); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t scatter_rows(Ctx &c, u32 n, const f64 *src, f64 *dst) {

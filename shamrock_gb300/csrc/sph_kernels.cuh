@@ -23,9 +23,11 @@ struct RowSpace {
     const f64 *x, *y, *z;
 };
 
-// Hydro fields in the same index space as the CSR entries.
+// Hydro fields in the same index space as the CSR entries.  alpha (optional): the
+// per-particle viscosity of the varying-AV form, else the constant alpha_AV.
 struct HydroSpace {
     const f64 *h, *u, *vx, *vy, *vz, *omega, *P, *cs;
+    const f64 *alpha;
 };
 
 // Equation of state of the step: adiabatic (P = (gamma - 1) rho u) or locally
@@ -79,6 +81,21 @@ cudaError_t kdk_correct64(Ctx &c, const LocalFields &lf, u32 n, const f64 *aox, 
                           const f64 *aoz, u32 avs, const f64 *du_old, f64 dt);
 cudaError_t cfl64(Ctx &c, u32 n, const f64 *h, const f64 *vsig, const f64 *ax, const f64 *ay,
                   const f64 *az, u32 avs, f64 C_cour, f64 C_force, f64 *dt_part);
+// varying (Cullen & Dehnen 2010) viscosity, sph64.cu:
+// div v, curl v, d(div v)/dt per pipeline row from rank-ordered fields (hs: h, v, omega;
+// ax..az: the accelerations of the last evaluation), outputs by local id
+cudaError_t velgrad64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, const f64 *ax,
+                      const f64 *ay, const f64 *az, f64 pmass, f64 *divv, f64 *cx, f64 *cy,
+                      f64 *cz, u32 cvs, f64 *dtdivv);
+// the switch update of n local particles (UpdateViscosity.cpp:170-215)
+cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64 *cy,
+                        const f64 *cz, u32 cvs, const f64 *dtdivv, const f64 *cs, const f64 *h,
+                        const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
+                        f64 *alpha_new);
+// dst[r] = src[(merged id of rank r) -> local source] * stride, r < N (ghosts copy their source)
+cudaError_t gather_merged64(Ctx &c, u32 N, u32 n_local, const f64 *src, u32 stride, f64 *dst);
+// dst[row_local[t]] = src[row_rank[t]] for the n pipeline rows
+cudaError_t rank_to_local64(Ctx &c, u32 n, const f64 *src_rank, f64 *dst);
 cudaError_t scatter_rows(Ctx &c, u32 n, const f64 *src, f64 *dst);
 cudaError_t gather_rows(Ctx &c, u32 n, const f64 *src_rank, f64 *dst, f64 *dst2);
 cudaError_t fill64(Ctx &c, u32 n, f64 *dst, f64 v);

@@ -147,6 +147,15 @@ __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__res
 // derivatives kernel.  c_s is stored in FP32, so it and the LP07 power are
 // evaluated in FP32 (relative error ~2e-7, the size of the records' own rounding); rho,
 // P and 1/(rho^2 Omega) stay FP64 until they are split into the record.
+// varying viscosity: the accelerations of the last evaluation as FP32 records (ghosts
+// copy their source) and the plain sound speed per rank (the records' c_s lane then
+// carries alpha c_s)
+struct StageAV {
+    const f64 *ax, *ay, *az; // caller's local fields, stride of the caller's vectors
+    float4 *A;               // null: constant viscosity
+    float *cs_rank;
+};
+
 struct StageEos {
     u32 kind;       // 0 adiabatic, 1 locally isothermal LP07
     f64 gm1;        // gamma - 1
@@ -161,7 +170,8 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
                                      const f64 *__restrict__ omega, f64 pmass, StageEos eos,
                                      const f64 *__restrict__ sx, const f64 *__restrict__ sy,
                                      const f64 *__restrict__ sz, float4 *__restrict__ P,
-                                     float4 *__restrict__ H, f64 *__restrict__ h_rank) {
+                                     float4 *__restrict__ H, f64 *__restrict__ h_rank,
+                                     StageAV av) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
     u32 id  = sort_index[r];
@@ -199,6 +209,11 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
     P[p2 + 1] = make_float4(xl, yl, zl, cs);
     H[p2]     = make_float4(vxh, vyh, vzh, __double2float_rn(uu));
     H[p2 + 1] = make_float4(Ph, c1, pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, Pl));
+    if (av.A) {
+        av.A[r]       = make_float4(__double2float_rn(av.ax[iv]), __double2float_rn(av.ay[iv]),
+                                    __double2float_rn(av.az[iv]), 0.f);
+        av.cs_rank[r] = cs;
+    }
 }
 
 // sum_b f(q) and sum_b (3 f + q f') over the row, q = r / h_a.  The next four entries
@@ -317,9 +332,12 @@ struct MixedParams {
 // with c1 = 1/(rho^2 Omega) and c2 = 1/(rho Omega) = c1 rho, rho = m (hfact/h)^3.
 // Self and coincident pairs (r = 0) contribute nothing and are skipped, which also
 // makes padding a partial batch of four with the row's own index harmless.
+// cs_rank (varying viscosity): the records' c_s lane holds alpha c_s, p.alpha_AV is 1,
+// and the plain c_s of the row for the v_sig maximum comes from cs_rank.
 __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
                                                u32 k0, u32 k1, const MixedParams &p, float &Fx,
-                                               float &Fy, float &Fz, float &U, float &vsig_max) {
+                                               float &Fy, float &Fz, float &U, float &vsig_max,
+                                               const float *__restrict__ cs_rank = nullptr) {
     const bool vec = rs.row_rank != nullptr;
     const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
     const F8 ha = ldg256(&ms.H[2 * (size_t) a]);
@@ -330,6 +348,7 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
     const float c1a = ha.b.y, c2a = c1a * rho_a;
     const float vla_x = bf_hi(ha.b.z), vla_y = bf_lo(ha.b.z), vla_z = bf_hi(ha.b.w);
     const float k4a = hia2 * hia2 * kNorm3dF;
+    const float cs_sig = cs_rank ? cs_rank[a] : cs_a;
     float cx = 0.f, cy = 0.f, cz = 0.f, cu = 0.f;
     Fx = Fy = Fz = U = 0.f;
     vsig_max = 0.f;
@@ -380,7 +399,7 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
             by += f * ry;
             bz += f * rz;
             bu += AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - hb[j].a.w) * (Fa * c2a + Fb * c2b);
-            vsig_max = fmaxf(vsig_max, cs_a + 2.f * avr);
+            vsig_max = fmaxf(vsig_max, cs_sig + 2.f * avr);
         }
         kahan_add(Fx, cx, bx);
         kahan_add(Fy, cy, by);
@@ -410,7 +429,8 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
                                                            MixedParams p, f64 pmass,
                                                            const f64 *__restrict__ h_rank, f64 hdt,
                                                            f64 C_cour, f64 C_force, LocalFields lf,
-                                                           ExtAccel ext, Scalars *sc) {
+                                                           ExtAccel ext, Scalars *sc,
+                                                           const float *__restrict__ cs_rank) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     u64 ev2 = 0, dtm = ~0ull;
     float v2 = 0.f;
@@ -418,7 +438,7 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
         u32 a  = rs.row_rank[t];
         u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
         float Fx, Fy, Fz, U, vm;
-        derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm);
+        derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm, cs_rank);
         f64 fx = -pmass * (f64) Fx, fy = -pmass * (f64) Fy, fz = -pmass * (f64) Fz;
         f64 tdu = pmass * (f64) U;
         u32 i     = rs.row_local[t];
@@ -460,6 +480,123 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
         atomicMin((unsigned long long *) &sc->dt_min, (unsigned long long) dtm);
         atomicAdd(&sc->sum_v2, (f64) v2);
     }
+}
+
+// ---- varying viscosity, FP32 pair arithmetic: div v, curl v (SPH estimates) and
+// d(div v)/dt = tr(G(a)) - tr(G(v) G(v)) with the corrected gradients G = R^-1 D, the
+// mass factoring out of R^-1 D.  Positions and velocities from the hi/lo records,
+// accelerations from the FP32 acceleration records; FP32 sums (the results feed the
+// viscosity switch, not the state).  Same pairs, kernel and order of terms as k_velgrad64.
+__device__ __forceinline__ void inv33f(const float m[3][3], float r[3][3]) {
+    const float a00 = m[0][0], a01 = m[0][1], a02 = m[0][2];
+    const float a10 = m[1][0], a11 = m[1][1], a12 = m[1][2];
+    const float a20 = m[2][0], a21 = m[2][1], a22 = m[2][2];
+    const float det = (((((-a02 * a11) * a20 + (a01 * a12) * a20) + (a02 * a10) * a21)
+                        - (a00 * a12) * a21) - (a01 * a10) * a22) + (a00 * a11) * a22;
+    const float id = __frcp_rn(det);
+    r[0][0] = (-a12 * a21 + a11 * a22) * id;
+    r[0][1] = (a02 * a21 - a01 * a22) * id;
+    r[0][2] = (-a02 * a11 + a01 * a12) * id;
+    r[1][0] = (a12 * a20 - a10 * a22) * id;
+    r[1][1] = (-a02 * a20 + a00 * a22) * id;
+    r[1][2] = (a02 * a10 - a00 * a12) * id;
+    r[2][0] = (-a11 * a20 + a10 * a21) * id;
+    r[2][1] = (a01 * a20 - a00 * a21) * id;
+    r[2][2] = (-a01 * a10 + a00 * a11) * id;
+}
+
+__global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace ms,
+                                                       const float4 *__restrict__ A,
+                                                       const f64 *__restrict__ omega_local,
+                                                       f64 pmass, float mh3,
+                                                       f64 *__restrict__ divv, f64 *__restrict__ cx,
+                                                       f64 *__restrict__ cy, f64 *__restrict__ cz,
+                                                       u32 cvs, f64 *__restrict__ dtdivv) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    const u32 a  = rs.row_rank[t];
+    const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
+    const F8 ha = ldg256(&ms.H[2 * (size_t) a]);
+    const float4 aa = __ldg(&A[a]);
+    const float hia = pa.a.w, hia2 = hia * hia;
+    const float k4a = hia2 * hia2 * kNorm3dF;
+    const float vla[3] = {bf_hi(ha.b.z), bf_lo(ha.b.z), bf_hi(ha.b.w)};
+    float sdiv = 0.f, sc[3] = {0.f, 0.f, 0.f};
+    float R[3][3] = {}, Dv[3][3] = {}, Da[3][3] = {};
+    for (u32 k = k0; k < k1; k++) {
+        const u32 b   = rs.ent[k];
+        const F8 pb   = ldg256(&ms.P[2 * (size_t) b]);
+        const float r[3] = {(pa.a.x - pb.a.x) + (pa.b.x - pb.b.x), (pa.a.y - pb.a.y) + (pa.b.y - pb.b.y),
+                            (pa.a.z - pb.a.z) + (pa.b.z - pb.b.z)};
+        const float r2  = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
+        const float hib = pb.a.w;
+        if (r2 * hia2 > 4.f && r2 * (hib * hib) > 4.f) continue;
+        const F8 hb      = ldg256(&ms.H[2 * (size_t) b]);
+        const float4 ab  = __ldg(&A[b]);
+        const float rab  = sqrtf(r2);
+        const float v[3] = {(ha.a.x - hb.a.x) + (vla[0] - bf_hi(hb.b.z)),
+                            (ha.a.y - hb.a.y) + (vla[1] - bf_lo(hb.b.z)),
+                            (ha.a.z - hb.a.z) + (vla[2] - bf_hi(hb.b.w))};
+        const float w[3] = {aa.x - ab.x, aa.y - ab.y, aa.z - ab.z};
+        const float inv  = (rab < 1e-9f) ? 0.f : __frcp_rn(rab);
+        const float F    = k4a * m4_df32(rab * hia) * inv; // dW(r, h_a) / r
+        const float g[3] = {F * r[0], F * r[1], F * r[2]};
+        sdiv  = sdiv + ((v[0] * g[0] + v[1] * g[1]) + v[2] * g[2]);
+        sc[0] = sc[0] + (v[1] * g[2] - v[2] * g[1]);
+        sc[1] = sc[1] + (v[2] * g[0] - v[0] * g[2]);
+        sc[2] = sc[2] + (v[0] * g[1] - v[1] * g[0]);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                R[i][j]  = R[i][j] - r[i] * g[j];
+                Dv[j][i] = Dv[j][i] - v[i] * g[j];
+                Da[j][i] = Da[j][i] - w[i] * g[j];
+            }
+    }
+    const u32 i = rs.row_local[t];
+    const float rho_a = mh3 * hia2 * hia;
+    const float f = -(float) pmass / (__double2float_rn(omega_local[i]) * rho_a);
+    divv[i] = (f64) (f * sdiv);
+    cx[(size_t) i * cvs] = (f64) (f * sc[0]);
+    cy[(size_t) i * cvs] = (f64) (f * sc[1]);
+    cz[(size_t) i * cvs] = (f64) (f * sc[2]);
+    float Ri[3][3], G[3][3];
+    inv33f(R, Ri);
+    float div_a = 0.f;
+#pragma unroll
+    for (int j = 0; j < 3; j++) div_a += (Ri[j][0] * Da[0][j] + Ri[j][1] * Da[1][j]) + Ri[j][2] * Da[2][j];
+#pragma unroll
+    for (int i2 = 0; i2 < 3; i2++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) G[i2][j] = (Ri[i2][0] * Dv[0][j] + Ri[i2][1] * Dv[1][j]) + Ri[i2][2] * Dv[2][j];
+    float tens = 0.f;
+#pragma unroll
+    for (int i2 = 0; i2 < 3; i2++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) tens += G[j][i2] * G[i2][j];
+    dtdivv[i] = (f64) (div_a - tens);
+}
+
+// P.b.w (c_s) times the updated alpha of each rank's source particle
+__global__ void k_stage_alpha(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
+                              const u32 *__restrict__ ghost_src, const f64 *__restrict__ alpha,
+                              float4 *__restrict__ P) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    u32 id  = sort_index[r];
+    u32 src = id < n_local ? id : ghost_src[id - n_local];
+    float *w = &((float *) &P[2 * (size_t) r + 1])[3];
+    *w       = *w * __double2float_rn(alpha[src]);
+}
+
+__global__ void k_cs_to_local(u32 n, const u32 *__restrict__ row_rank,
+                              const u32 *__restrict__ row_local, const float *__restrict__ cs_rank,
+                              f64 *__restrict__ dst) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    dst[row_local[t]] = (f64) cs_rank[row_rank[t]];
 }
 
 MixedParams mixed_params(f64 pmass, f64 alpha_u, f64 alpha_AV, f64 beta_AV) {
@@ -510,7 +647,16 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
 }
 
 cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
-                               const f64 *omega_local, f64 pmass, const EosParams &eos) {
+                               const f64 *omega_local, f64 pmass, const EosParams &eos,
+                               bool varying_av) {
+    StageAV av{lf.ax, lf.ay, lf.az, nullptr, nullptr};
+    if (varying_av) {
+        cudaError_t e;
+        if ((e = c.f_aux1.ensure(sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
+        if ((e = c.f_aux2.ensure(sizeof(float) * (size_t) N, c.stream)) != cudaSuccess) return e;
+        av.A       = c.f_aux1.as<float4>();
+        av.cs_rank = c.f_aux2.as<float>();
+    }
     StageEos se{eos.kind, eos.gamma - 1, pmass * kHfact * kHfact * kHfact,
                 (float) (eos.gamma * (eos.gamma - 1)), (float) (1.0 / (eos.r0 * eos.r0)),
                 (float) (eos.cs0 * eos.cs0), (float) -eos.q};
@@ -518,19 +664,44 @@ cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf
     { k_gather_stage_mixed<<<div_up(N, 256), 256, 0, c.stream>>>(
         c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf, omega_local, pmass, se,
         c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.f_pos.as<float4>(),
-        c.f_aux0.as<float4>(), c.sh2.as<f64>()); GBSPH_COUNTED; }
+        c.f_aux0.as<float4>(), c.sh2.as<f64>(), av); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
                               f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
-                              const LocalFields &lf, const ExtAccel &ext) {
+                              const LocalFields &lf, const ExtAccel &ext, bool varying_av) {
     MixedSpace ms = mixed_space(c, c.n_obj);
-    MixedParams p = mixed_params(pmass, alpha_u, alpha_AV, beta_AV);
+    MixedParams p = mixed_params(pmass, alpha_u, varying_av ? 1.0 : alpha_AV, beta_AV);
+    const float *cs_rank = varying_av ? c.f_aux2.as<float>() : nullptr;
     ProfScope ps(c, kProfDerivs, rs.n);
     { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, c.sh2.as<f64>(), hdt, C_cour,
                                                                  C_force, lf, ext,
-                                                                 c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+                                                                 c.d_scalars.as<Scalars>(),
+                                                                 cs_rank); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t velgrad_mixed(Ctx &c, const RowSpace &rs, const f64 *omega_local, f64 pmass,
+                          f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv) {
+    MixedSpace ms = mixed_space(c, c.n_obj);
+    ProfScope ps(c, kProfVelGrad, rs.n);
+    { k_velgrad_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(
+        rs, ms, c.f_aux1.as<float4>(), omega_local, pmass, (float) (pmass * kHfact * kHfact * kHfact),
+        divv, cx, cy, cz, cvs, dtdivv); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t stage_alpha_mixed(Ctx &c, u32 N, u32 n_local, const f64 *alpha_local) {
+    { k_stage_alpha<<<div_up(N, 256), 256, 0, c.stream>>>(c.sort_index.as<u32>(), N, n_local,
+                                                         c.ghost_src.as<u32>(), alpha_local,
+                                                         c.f_pos.as<float4>()); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t cs_to_local_mixed(Ctx &c, u32 n, f64 *dst) {
+    { k_cs_to_local<<<div_up(n, 256), 256, 0, c.stream>>>(n, c.row_rank.as<u32>(), c.row_local.as<u32>(),
+                                                         c.f_aux2.as<float>(), dst); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 

@@ -32,11 +32,21 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
 // + the FP64 rank-ordered copies in the mixed path; only h is kept in FP64, in c.sh2),
 // then the fused derivatives step, which reads the records, c.sh2 and the caller's
 // local fields
+// varying_av: also stage FP32 acceleration records and the plain c_s per rank
 cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
-                               const f64 *omega_local, f64 pmass, const EosParams &eos);
+                               const f64 *omega_local, f64 pmass, const EosParams &eos,
+                               bool varying_av = false);
+// varying_av: per-particle alpha folded into the records' c_s lane (stage_alpha_mixed)
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
                               f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
-                              const LocalFields &lf, const ExtAccel &ext);
+                              const LocalFields &lf, const ExtAccel &ext, bool varying_av = false);
+// varying viscosity: div v, curl v, d(div v)/dt per row (outputs by local id), after
+// gather_stage_mixed(..., true); alpha of the local particles into the records; the
+// staged plain c_s back to local order
+cudaError_t velgrad_mixed(Ctx &c, const RowSpace &rs, const f64 *omega_local, f64 pmass,
+                          f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv);
+cudaError_t stage_alpha_mixed(Ctx &c, u32 N, u32 n_local, const f64 *alpha_local);
+cudaError_t cs_to_local_mixed(Ctx &c, u32 n, f64 *dst);
 cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                                 f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
                                 f64 *du, f64 *vsig);

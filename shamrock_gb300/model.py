@@ -21,6 +21,10 @@ from . import _lib as L
 
 FIELDS_VEC = ("xyz", "vxyz", "axyz")
 FIELDS_SCAL = ("hpart", "uint", "duint")
+# fields of the varying (CD10) viscosity: state alpha_AV and soundspeed, diagnostics
+# divv, curlv, dtdivv (the reference adds them to the layout for that AV only)
+FIELDS_AV_SCAL = ("alpha_AV", "soundspeed", "divv", "dtdivv")
+FIELDS_AV_VEC = ("curlv",)
 
 
 class SolverConfig:
@@ -53,10 +57,15 @@ class SolverConfig:
                        beta_AV=float(beta_AV))
 
     def set_artif_viscosity_VaryingMM97(self, **kw):
-        raise NotImplementedError("only constant artificial viscosity is on the GB300 path")
+        raise NotImplementedError("the Morris & Monaghan (1997) switch is not on the GB300 path "
+                                  "(constant and VaryingCD10 are)")
 
-    def set_artif_viscosity_VaryingCD10(self, **kw):
-        raise NotImplementedError("only constant artificial viscosity is on the GB300 path")
+    def set_artif_viscosity_VaryingCD10(self, *, alpha_min, alpha_max, sigma_decay, alpha_u,
+                                        beta_AV):
+        """Cullen & Dehnen (2010) switch (pySPHModel.cpp:171-186, UpdateViscosity.cpp)."""
+        self.av = dict(type="cd10", alpha_min=float(alpha_min), alpha_max=float(alpha_max),
+                       sigma_decay=float(sigma_decay), alpha_u=float(alpha_u),
+                       beta_AV=float(beta_AV), alpha_AV=0.0)
 
     def set_boundary_periodic(self):
         self.boundary = "periodic"
@@ -163,8 +172,8 @@ class Model:
         self.cfg = SolverConfig()
         self.box_min = np.zeros(3)
         self.box_max = np.ones(3)
-        self._host = {k: np.zeros((0, 3)) for k in FIELDS_VEC}
-        self._host.update({k: np.zeros(0) for k in FIELDS_SCAL})
+        self._host = {k: np.zeros((0, 3)) for k in FIELDS_VEC + FIELDS_AV_VEC}
+        self._host.update({k: np.zeros(0) for k in FIELDS_SCAL + FIELDS_AV_SCAL})
         self._dev = None  # dict of torch tensors once uploaded
         self._omega = None
         self.time = 0.0
@@ -234,6 +243,9 @@ class Model:
         self._host["hpart"] = np.concatenate([self._host["hpart"], np.asarray(hpart, float)])
         self._host["uint"] = np.concatenate([self._host["uint"], np.asarray(upart, float)])
         self._host["duint"] = np.concatenate([self._host["duint"], np.zeros(n)])
+        for k in FIELDS_AV_SCAL:
+            self._host[k] = np.concatenate([self._host[k], np.zeros(n)])
+        self._host["curlv"] = np.concatenate([self._host["curlv"], np.zeros((n, 3))])
 
     def add_cube_fcc_3d(self, dr, box_min, box_max):
         """Close-packed lattice of the reference's add_particles_fcc
@@ -253,8 +265,10 @@ class Model:
         pos = pos[keep]
         self.push_particle(pos, np.full(len(pos), 2 * dr), np.zeros(len(pos)))
 
-    def set_particles(self, pos, vel=None, h=None, u=None):
-        """Replace all particles (host arrays); h defaults to hfact*(m/rho=1)^(1/3)."""
+    def set_particles(self, pos, vel=None, h=None, u=None, alpha=None):
+        """Replace all particles (host arrays); h defaults to hfact*(m/rho=1)^(1/3); the
+        varying-viscosity fields start at zero (alpha_AV = alpha if given), as the
+        reference's zero-initialised fields."""
         pos = np.asarray(pos, float).reshape(-1, 3)
         n = pos.shape[0]
         self._dev = None
@@ -263,6 +277,11 @@ class Model:
             axyz=np.zeros((n, 3)),
             hpart=np.full(n, 1.2 * (1.0 / n) ** (1 / 3)) if h is None else np.asarray(h, float).copy(),
             uint=np.zeros(n) if u is None else np.asarray(u, float).copy(), duint=np.zeros(n))
+        for k in FIELDS_AV_SCAL:
+            self._host[k] = np.zeros(n)
+        self._host["curlv"] = np.zeros((n, 3))
+        if alpha is not None:
+            self._host["alpha_AV"] = np.broadcast_to(np.asarray(alpha, float), (n,)).copy()
 
     def _field_host(self, name):
         self._to_host()
@@ -300,9 +319,9 @@ class Model:
             return self._dev
         dev = torch.device("cuda", self.ctx_py.device if self.ctx_py else 0)
         d = {}
-        for k in FIELDS_VEC:
+        for k in FIELDS_VEC + FIELDS_AV_VEC:
             d[k] = torch.as_tensor(np.ascontiguousarray(self._host[k].T), device=dev).contiguous()
-        for k in FIELDS_SCAL:
+        for k in FIELDS_SCAL + FIELDS_AV_SCAL:
             d[k] = torch.as_tensor(self._host[k], device=dev).contiguous()
         d["omega"] = torch.ones_like(d["hpart"])
         self._dev = d
@@ -311,9 +330,9 @@ class Model:
     def _to_host(self):
         if self._dev is None:
             return
-        for k in FIELDS_VEC:
+        for k in FIELDS_VEC + FIELDS_AV_VEC:
             self._host[k] = self._dev[k].T.cpu().numpy().copy()
-        for k in FIELDS_SCAL:
+        for k in FIELDS_SCAL + FIELDS_AV_SCAL:
             self._host[k] = self._dev[k].cpu().numpy().copy()
         self._omega = self._dev["omega"].cpu().numpy().copy()
         self._dev = None
@@ -325,8 +344,8 @@ class Model:
     def collect_data(self):
         """Host copy of the particle fields, keyed as the reference's ctx.collect_data()."""
         if self._dev is not None:
-            out = {k: self._dev[k].T.cpu().numpy().copy() for k in FIELDS_VEC}
-            out.update({k: self._dev[k].cpu().numpy().copy() for k in FIELDS_SCAL})
+            out = {k: self._dev[k].T.cpu().numpy().copy() for k in FIELDS_VEC + FIELDS_AV_VEC}
+            out.update({k: self._dev[k].cpu().numpy().copy() for k in FIELDS_SCAL + FIELDS_AV_SCAL})
             out["omega"] = self._dev["omega"].cpu().numpy().copy()
             return out
         out = {k: v.copy() for k, v in self._host.items()}
@@ -347,6 +366,13 @@ class Model:
         p.uint = d["uint"].data_ptr()
         p.duint = d["duint"].data_ptr()
         p.omega = d["omega"].data_ptr()
+        if self.cfg.av["type"] == "cd10":
+            p.alpha_AV = d["alpha_AV"].data_ptr()
+            p.soundspeed = d["soundspeed"].data_ptr()
+            p.divv = d["divv"].data_ptr()
+            p.dtdivv = d["dtdivv"].data_ptr()
+            t = d["curlv"]
+            p.curlv = L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0)
         return p
 
     def _config_struct(self):
@@ -374,6 +400,10 @@ class Model:
             s.constant_G = c.constant_G
         s.pmass = c.gpart_mass
         s.alpha_u, s.alpha_AV, s.beta_AV = c.av["alpha_u"], c.av["alpha_AV"], c.av["beta_AV"]
+        if c.av["type"] == "cd10":
+            s.av_kind = L.GBSPH_AV_VARYING_CD10
+            s.alpha_min, s.alpha_max = c.av["alpha_min"], c.av["alpha_max"]
+            s.sigma_decay = c.av["sigma_decay"]
         s.cfl_cour, s.cfl_force = c.cfl_cour, c.cfl_force
         s.cfl_mult_stiffness = c.cfl_multiplier_stiffness
         s.htol_up_coarse, s.htol_up_fine = c.htol_up_coarse_cycle, c.htol_up_fine_cycle
