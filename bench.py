@@ -43,12 +43,14 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--workload", default="sedov",
-                   choices=["sedov", "sedov_plain", "clustered", "soundwave", "disc"],
+                   choices=["sedov", "sedov_plain", "clustered", "soundwave", "disc", "homogeneous"],
                    help="sedov: jittered Sedov-Taylor (default, 4*cells^3); sedov_plain: the "
                         "same without jitter; clustered: 8,388,608 particles, half uniform, "
                         "half in a Gaussian clump; soundwave: 64^3 travelling sound wave; "
                         "disc: 4,194,304-particle Keplerian disc (locally isothermal EOS, "
-                        "central point mass, free boundary)")
+                        "central point mass, free boundary); homogeneous: the reference's own "
+                        "SPH benchmark, 33,848,064-particle HCP box, varying CD10 viscosity, "
+                        "dt = 0 steps")
     p.add_argument("--cells", type=int, default=64, help="FCC cells per axis (4*cells^3 particles)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -64,6 +66,14 @@ def workload(cells, kind="sedov"):
     dataset is involved).  Returns (set-up dict, name, alpha_AV)."""
     from shamrock_gb300 import setups
 
+    if kind == "homogeneous":
+        s = homogeneous_setup(1 << 25)
+        name = ("homogeneous_hcp_box_%d (the reference's examples/benchmarks/"
+                "sph_homogeneous_benchmark.py: HCP lattice in the periodic box it closes, rho 1, "
+                "u = 0 but a central injection u_inj W(r, 16 dr), gamma 5/3, M4, varying CD10 "
+                "viscosity alpha in [0, 1] sigma 0.1 alpha_u 1 beta 2, CFL 0.1, every step "
+                "with dt = 0 as its set_next_dt(0.0), tree rebuilt every step)" % len(s["h"]))
+        return s, name, 0.0
     if kind == "clustered":
         s = setups.clustered_box(8388608, seed=12345, sigma=0.05)
         name = ("clustered_box_8388608 (half uniform, half Gaussian clump sigma 0.05, "
@@ -88,13 +98,39 @@ def workload(cells, kind="sedov"):
     return s, name, 1.0
 
 
+def homogeneous_setup(n_target):
+    from shamrock_gb300 import setups
+
+    s = setups.homogeneous_box(n_target)
+    s.update(av="cd10", cfl=0.1, dt_zero=True)
+    return s
+
+
+def step(m, s, **kw):
+    """One evolve_once; the homogeneous benchmark sets the next dt to 0 before each."""
+    if s.get("dt_zero"):
+        m.dt = 0.0
+    return m.evolve_once(**kw)
+
+
+def ostep(sim, s):
+    if s.get("dt_zero"):
+        t, _, cm = sim.get_time()
+        sim.set_time(t, 0.0, cm)
+    return sim.evolve_once()
+
+
 def make_model(s, precision, device=0, alpha_AV=1.0):
     import shamrock_gb300 as sg
 
     ctx = sg.Context(device)
     m = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
     cfg = m.gen_default_config()
-    cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0)
+    if s.get("av") == "cd10":
+        cfg.set_artif_viscosity_VaryingCD10(alpha_min=0.0, alpha_max=1.0, sigma_decay=0.1,
+                                            alpha_u=1.0, beta_AV=2.0)
+    else:
+        cfg.set_artif_viscosity_Constant(alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0)
     if s.get("periodic", True):
         cfg.set_boundary_periodic()
     else:
@@ -110,8 +146,8 @@ def make_model(s, precision, device=0, alpha_AV=1.0):
     m.set_solver_config(cfg)
     m.resize_simulation_box(s["box_min"], s["box_max"])
     m.set_particles(s["pos"], s["vel"], s["h"], s["u"])
-    m.set_cfl_cour(0.3)
-    m.set_cfl_force(0.3)
+    m.set_cfl_cour(s.get("cfl", 0.3))
+    m.set_cfl_force(s.get("cfl", 0.3))
     return m
 
 
@@ -280,8 +316,9 @@ def reference_rank_runs(world, rank):
 def oracle_config(O, s, alpha_AV):
     """The oracle's configuration of workload `s` (same solver settings as make_model)."""
     disc = "cs0" in s
+    cfl = s.get("cfl", 0.3)
     oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=alpha_AV, beta_AV=2.0,
-                     cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
+                     cfl_cour=cfl, cfl_force=cfl, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
                      htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
                      h_max_subcycles=100, tree_reduction_level=3,
                      periodic=1 if s.get("periodic", True) else 0)
@@ -289,6 +326,8 @@ def oracle_config(O, s, alpha_AV):
         oc.eos_kind, oc.ext_kind = 1, 1
         oc.cs0, oc.eos_r0, oc.eos_q = s["cs0"], s["r0"], s["q"]
         oc.central_mass, oc.constant_G = s["M"], s["G"]
+    if s.get("av") == "cd10":
+        oc.av_kind, oc.alpha_min, oc.alpha_max, oc.sigma_decay = 1, 0.0, 1.0, 0.1
     oc.bmin[:] = list(s["box_min"])
     oc.bmax[:] = list(s["box_max"])
     return oc
@@ -301,6 +340,7 @@ def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     if threads:
         O.set_threads(threads)
     cores = O.get_threads()
+    s, what = cpu_sample(s)
     oc = oracle_config(O, s, alpha_AV)
     sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
     sim.evolve_once()  # dt = 0 step (h convergence, first CFL), untimed
@@ -308,14 +348,22 @@ def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     t0 = time.time()
     steps = 0
     while True:
-        sim.evolve_once()
+        ostep(sim, s)
         steps += 1
         if time.time() - t0 >= seconds:
             break
     el = time.time() - t0
     return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{steps} FP64 oracle steps of the full workload ({n} particles) after one "
+            "sample": f"{steps} FP64 oracle steps of {what} ({n} particles) after one "
                       f"untimed dt=0 step, {el:.1f} s, OpenMP {cores} threads"}
+
+
+def cpu_sample(s):
+    """The CPU arms time the full workload, except the 33.8M-particle homogeneous box (one
+    oracle step of it takes minutes): there the same set-up at 2^20 target particles."""
+    if s.get("dt_zero"):
+        return homogeneous_setup(1 << 20), "the same homogeneous set-up at 2^20 target particles"
+    return s, "the full workload"
 
 
 def run_reference(args):
@@ -328,22 +376,23 @@ def run_reference(args):
 
     O.set_threads(os.cpu_count())
     cores = O.get_threads()
+    s, what = cpu_sample(s)
     oc = oracle_config(O, s, alpha_av)
     sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
     n = len(s["h"])
     for _ in range(max(1, min(args.warmup, 2))):
-        sim.evolve_once()
+        ostep(sim, s)
     budget = 150.0
     t0 = time.time()
     steps = 0
     while steps < args.steps:
-        sim.evolve_once()
+        ostep(sim, s)
         steps += 1
         if time.time() - t0 > budget:
             break
     el = time.time() - t0
     value = n * steps / el
-    sample = (f"{steps} of {args.steps} requested FP64 steps of the full workload ({n} particles; "
+    sample = (f"{steps} of {args.steps} requested FP64 steps of {what} ({n} particles; "
               f"stopped at a {budget:.0f} s budget if reached), after "
               f"{max(1, min(args.warmup, 2))} untimed warm-up steps")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -401,7 +450,7 @@ def run_gb300(args):
     m = make_model(s, args.precision, device=local, alpha_AV=alpha_av)
     lib = m._lib()
     for _ in range(max(args.warmup, 3)):
-        m.evolve_once()
+        step(m, s)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -414,7 +463,7 @@ def run_gb300(args):
     with ClockSampler(local) as clocks:
         e0.record(stream)
         for _ in range(args.steps):
-            logs.append(m.evolve_once(stream=None))
+            logs.append(step(m, s, stream=None))
         e1.record(stream)
         torch.cuda.synchronize()
     if dist:
@@ -433,6 +482,8 @@ def run_gb300(args):
     if not args.no_e2e:
         d = m._to_device()
         names = ("xyz", "vxyz", "axyz", "hpart", "uint", "duint")
+        if s.get("av") == "cd10":
+            names = names + ("alpha_AV", "soundspeed")
         host = {k: torch.empty(d[k].shape, dtype=torch.float64, pin_memory=True) for k in names}
         for k in names:
             host[k].copy_(d[k])
@@ -444,7 +495,7 @@ def run_gb300(args):
         for _ in range(steps_e2e):
             for k in names:
                 d[k].copy_(host[k], non_blocking=True)
-            m.evolve_once()
+            step(m, s)
             for k in names:
                 host[k].copy_(d[k], non_blocking=True)
         f1.record(stream)
@@ -475,18 +526,24 @@ def run_gb300(args):
         "step_log": {k: log[k] for k in ("h_subcycles", "h_iterations", "corrector_iters",
                                           "next_dt", "cfl_mult")},
     }
+    if args.workload == "homogeneous":
+        # the reference's own published figure for this set-up (FP64, varying CD10 AV,
+        # 33,848,064 particles, one H100): examples/benchmarks/sph_homogeneous_bench_result.json
+        line["published_reference"] = {
+            "value": 25502056.0, "unit": UNIT, "hardware": "NVIDIA H100, DPC++, 1 rank",
+            "precision": "fp64", "this_over_published": value / 25502056.0}
     if world == 1 and not args.no_accuracy:
         line["accuracy_mixed_vs_fp64"] = accuracy(s, alpha_AV=alpha_av)
         # FP64 GPU rate on the same workload (the x3 denominator), a few steps
         m64 = make_model(s, "fp64", alpha_AV=alpha_av)
         for _ in range(2):
-            m64.evolve_once()
+            step(m64, s)
         torch.cuda.synchronize()
         g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         k64 = 3
         g0.record(stream)
         for _ in range(k64):
-            m64.evolve_once()
+            step(m64, s)
         g1.record(stream)
         torch.cuda.synchronize()
         v64 = n * k64 / (g0.elapsed_time(g1) * 1e-3)

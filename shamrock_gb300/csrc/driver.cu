@@ -57,7 +57,7 @@ void prof_collect(Ctx &c) {
 Ctx::~Ctx() {
     for (cudaEvent_t e : prof.pool) cudaEventDestroy(e);
     DevBuf *bufs[] = {&scan_scratch, &d_scalars, &d_bbox, &keys, &sort_index, &flags_a, &flags_b,
-                      &offsets, &reduc, &reduced, &lchild, &rchild, &lflag, &rflag, &endrange,
+                      &offsets, &reduc, &reduced, &radix_k, &radix_v, &radix_hist, &radix_off, &lchild, &rchild, &lflag, &rflag, &endrange,
                       &parent, &boxes, &visit, &fboxes, &fpairs, &rank_of, &sx, &sy, &sz, &sh, &row_rank,
                       &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
                       &owner, &leaf_thr, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
@@ -646,7 +646,7 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         u32 N = n + c.n_ghost;
         CU(bbox_from_merged(c, N));
         CU(tree_build(c, c.mx.as<f64>(), c.my.as<f64>(), c.mz.as<f64>(), c.mh.as<f64>(), N,
-                      cfg->tree_reduction_level, cfg->htol_up_coarse, 32, 0));
+                      cfg->tree_reduction_level, cfg->htol_up_coarse, 32, 0, true));
         CU(build_rows(c, n));
         if (mixed) {
             CU(stage_positions_mixed(c, N, cfg->htol_up_coarse));

@@ -39,7 +39,7 @@ struct Scalars {
     u32 flags;         // error flags raised by kernels
     u32 leaf_cnt_max;  // largest stage-1 list among leaves that overflowed their slots
     u32 row_cnt_max;   // largest stage-2 row among rows that overflowed their slots
-    u32 pad;
+    u32 dup_keys;      // radix-sorted Morton keys had equal neighbours
 };
 
 enum KernelFlags : u32 {
@@ -111,6 +111,7 @@ struct Ctx {
     int key_bits = 32;
     u32 n_obj = 0, morton_count = 0, leaf_count = 0;
     DevBuf keys, sort_index, flags_a, flags_b, offsets, reduc, reduced;
+    DevBuf radix_k, radix_v, radix_hist, radix_off; // radix sort ping-pong and digit tables
     DevBuf lchild, rchild, lflag, rflag, endrange, parent, boxes, visit, fboxes, fpairs;
     bool has_rint = false;
 
@@ -123,6 +124,7 @@ struct Ctx {
     // ---- neighbour cache
     u64 leaf_csr_total = 0, csr_total = 0;
     u32 leaf_cap = 0, row_cap = 0; // one-pass slots per leaf / row (grown on overflow)
+    u32 row_seen = 0;              // largest stage-2 row of the last build
     u64 slot_budget = 0;            // bytes of one-pass slots allowed (0: library default)
     DevBuf leaf_cnt, leaf_off, leaf_ent; // stage 1 (leaf ids)
     DevBuf owner;                        // per row: leaf index
@@ -176,8 +178,11 @@ struct ProfScope {
 // All return cudaError_t and enqueue work on ctx.stream.
 
 // tree.cu
+// fast_sort: sort the n real keys with the radix sort (the permutation equals the bitonic
+// network's whenever the keys are distinct, which it checks; the padding's order is not
+// kept, so only builds whose sorted padding is never exported may ask for it)
 cudaError_t tree_build(Ctx &c, const f64 *x, const f64 *y, const f64 *z, const f64 *h, u32 n,
-                       u32 level, f64 htol, int key_bits, u32 morton_count);
+                       u32 level, f64 htol, int key_bits, u32 morton_count, bool fast_sort = false);
 cudaError_t set_bbox_host(Ctx &c, const f64 *bmin, const f64 *bmax);
 cudaError_t bbox_from_merged(Ctx &c, u32 n); // reduce mx/my/mz -> widened d_bbox
 cudaError_t sync_scalars(Ctx &c);            // copy Scalars to pinned host, wait

@@ -456,11 +456,13 @@ __global__ void __launch_bounds__(256) k_part_cache(
         if (MODE == kCount) off[row] = (c + 3u) & ~3u;
         if (MODE == kOnePass) {
             off[row] = w;
-            if (c > cap) {
-                atomicOr(&sc->flags, kFlagCsrCap);
-                atomicMax(&sc->row_cnt_max, c);
-            }
+            if (c > cap) atomicOr(&sc->flags, kFlagCsrCap);
         }
+    }
+    // the largest row of the build (sizes the slots of the next one)
+    {
+        u64 m = block_reduce((u64) c, OpMaxU64{}, 0ull);
+        if (threadIdx.x == 0 && m) atomicMax(&sc->row_cnt_max, (u32) m);
     }
     if (MODE != kCount) {
         u64 tot = block_reduce((u64) c, OpAddU64{}, 0ull);
@@ -634,6 +636,12 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
     // the padded one-pass layout needs row * cap to fit the u32 offsets
     if (c.row_cap == 0) c.row_cap = kRowCap;
     auto slots_fit = [&](u32 cap) { return slots_ok(n, cap); };
+    // slots that no longer fit (more rows than before): size them from the largest row
+    // of the last build, with a quarter of margin, before falling back to two passes
+    if (!slots_fit(c.row_cap) && c.row_seen > 0) {
+        const u32 cap = (c.row_seen + c.row_seen / 4 + 7u) & ~3u;
+        if (cap < c.row_cap && slots_fit(cap)) c.row_cap = cap;
+    }
     bool one_pass = slots_fit(c.row_cap);
     if (one_pass)
         if ((e = c.csr_ent.ensure(sizeof(u32) * ((size_t) n * c.row_cap + 4), s)) != cudaSuccess) return e;
@@ -702,6 +710,7 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         if ((e = sync_scalars(c)) != cudaSuccess) return e;
         c.csr_total = c.h_scalars->csr_entries;
     }
+    c.row_seen    = c.h_scalars->row_cnt_max;
     c.cache_valid = true;
     return cudaGetLastError();
 }

@@ -13,6 +13,9 @@
 
 #include "gbsph_ctx.cuh"
 
+#include <type_traits>
+#include <utility>
+
 namespace gbsph {
 
 namespace {
@@ -189,6 +192,98 @@ cudaError_t bitonic_sort(K *keys, u32 *vals, u32 len, cudaStream_t s) {
         }
         { k_bitonic_smem<K, TILE><<<len / TILE, 512, 0, s>>>(keys, vals, TILE, length, length << 1,
                                                           TILE / 2); GBSPH_COUNTED; }
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- radix sort
+// Stable LSD radix sort of n u32 keys with u32 values, four 8-bit digits.  Per pass: a
+// per-block digit histogram (bucket-major), its exclusive scan (the global start of each
+// block's elements of each digit), and a scatter that walks the block's tile in index
+// order, 256 elements per round: lanes with equal digits are ranked with a warp match,
+// warps by an exclusive prefix of their per-warp counts, so every pass is stable.  With
+// distinct keys the result is the unique sorted order, hence the bitonic network's.
+constexpr u32 kRadixItems = 8, kRadixTile = 256 * kRadixItems;
+
+__global__ void __launch_bounds__(256) k_radix_hist(const u32 *__restrict__ keys, u32 n, int shift,
+                                                    u32 nblocks, u32 *__restrict__ hist) {
+    __shared__ u32 h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const u32 base = blockIdx.x * kRadixTile;
+#pragma unroll
+    for (u32 r = 0; r < kRadixItems; r++) {
+        const u32 i = base + r * 256 + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) k_radix_scatter(const u32 *__restrict__ kin,
+                                                       const u32 *__restrict__ vin, u32 n, int shift,
+                                                       u32 nblocks, const u32 *__restrict__ offs,
+                                                       u32 *__restrict__ kout, u32 *__restrict__ vout) {
+    __shared__ u32 cnt[256];   // next output slot of each digit for this block
+    __shared__ u32 wc[8][256]; // per-warp digit counts, then their exclusive prefix
+    const u32 t = threadIdx.x, lane = t & 31u, w = t >> 5;
+    cnt[t]         = offs[t * nblocks + blockIdx.x];
+    const u32 base = blockIdx.x * kRadixTile;
+    for (u32 r = 0; r < kRadixItems; r++) {
+        for (u32 k = lane; k < 256; k += 32) wc[w][k] = 0;
+        __syncthreads();
+        const u32 i     = base + r * 256 + t;
+        const bool valid = i < n;
+        const u32 key   = valid ? kin[i] : 0u;
+        const u32 val   = valid ? vin[i] : 0u;
+        const u32 d     = (key >> shift) & 255u;
+        // invalid lanes match only themselves (values above 255)
+        const u32 peers = __match_any_sync(0xffffffffu, valid ? d : (0x100u | lane));
+        const u32 lower = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lower == 0) wc[w][d] = __popc(peers);
+        __syncthreads();
+        u32 run = cnt[t];
+#pragma unroll
+        for (u32 ww = 0; ww < 8; ww++) {
+            const u32 c = wc[ww][t];
+            wc[ww][t]   = run;
+            run += c;
+        }
+        cnt[t] = run;
+        __syncthreads();
+        if (valid) {
+            const u32 pos = wc[w][d] + lower;
+            kout[pos]     = key;
+            vout[pos]     = val;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_adjacent_dup(const u32 *__restrict__ keys, u32 n, u32 *__restrict__ flag) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 < n && keys[i] == keys[i + 1]) atomicOr(flag, 1u);
+}
+
+// sorts keys[0..n) / vals[0..n) in place (four passes end in the input buffers)
+cudaError_t radix_sort_u32(Ctx &c, u32 *keys, u32 *vals, u32 n, cudaStream_t s) {
+    cudaError_t e;
+    if (n < 2) return cudaSuccess;
+    const u32 nb = div_up(n, kRadixTile);
+    if ((e = c.radix_k.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
+    if ((e = c.radix_v.ensure(sizeof(u32) * (size_t) n, s)) != cudaSuccess) return e;
+    if ((e = c.radix_hist.ensure(sizeof(u32) * 256 * (size_t) nb, s)) != cudaSuccess) return e;
+    if ((e = c.radix_off.ensure(sizeof(u32) * 256 * (size_t) nb, s)) != cudaSuccess) return e;
+    Scalars *dsc = c.d_scalars.as<Scalars>();
+    u32 *ka = keys, *va = vals, *kb = c.radix_k.as<u32>(), *vb = c.radix_v.as<u32>();
+    for (int shift = 0; shift < 32; shift += 8) {
+        { k_radix_hist<<<nb, 256, 0, s>>>(ka, n, shift, nb, c.radix_hist.as<u32>()); GBSPH_COUNTED; }
+        if ((e = scan_exclusive_u32(c.radix_hist.as<u32>(), c.radix_off.as<u32>(), 256 * nb,
+                                    &dsc->total2, c.scan_scratch, s)) != cudaSuccess)
+            return e;
+        { k_radix_scatter<<<nb, 256, 0, s>>>(ka, va, n, shift, nb, c.radix_off.as<u32>(), kb, vb); GBSPH_COUNTED; }
+        std::swap(ka, kb);
+        std::swap(va, vb);
     }
     return cudaGetLastError();
 }
@@ -413,7 +508,7 @@ __global__ void k_bbox_finalize(const Scalars *sc, BBox *bb, u32 val_count) {
 
 template<class K>
 cudaError_t tree_build_impl(Ctx &c, const f64 *x, const f64 *y, const f64 *z, const f64 *h, u32 n,
-                            u32 level, f64 htol, u32 morton_count) {
+                            u32 level, f64 htol, u32 morton_count, bool fast_sort) {
     cudaStream_t s = c.stream;
     cudaError_t e;
     u32 P = morton_count;
@@ -443,30 +538,41 @@ cudaError_t tree_build_impl(Ctx &c, const f64 *x, const f64 *y, const f64 *z, co
     K *keys = c.keys.as<K>();
     u32 *vals = c.sort_index.as<u32>();
     const u32 T = 256;
-    {
-        ProfScope ps(c, kProfSort, P);
-        { k_morton<K><<<div_up(P, T), T, 0, s>>>(x, y, z, n, P, c.d_bbox.as<BBox>(), keys, vals); GBSPH_COUNTED; }
-        if ((e = bitonic_sort<K>(keys, vals, P, s)) != cudaSuccess) return e;
-    }
-    int prof_tree = c.prof.on ? prof_begin(c, kProfTree, n) : -1;
-
-    // leaf reduction: ping-pong split tables, final table is a for even levels
-    u8 *fa = c.flags_a.as<u8>(), *fb = c.flags_b.as<u8>();
-    { k_split<K><<<div_up(n, T), T, 0, s>>>(keys, n, fa); GBSPH_COUNTED; }
-    for (u32 it = 1; it <= level; it++) {
-        if (it % 2 == 0) { k_reduce_iter<K><<<div_up(n, T), T, 0, s>>>(keys, n, fb, fa); GBSPH_COUNTED; }
-        else { k_reduce_iter<K><<<div_up(n, T), T, 0, s>>>(keys, n, fa, fb); GBSPH_COUNTED; }
-    }
-    u8 *fin = (level % 2 == 0) ? fa : fb;
     Scalars *dsc = c.d_scalars.as<Scalars>();
-    if ((e = scan_exclusive_flags(fin, c.offsets.as<u32>(), n, &dsc->total, c.scan_scratch, s)) !=
-        cudaSuccess)
-        return e;
-    { k_compact_leaves<K><<<div_up(n, T), T, 0, s>>>(fin, c.offsets.as<u32>(), n, keys,
-                                                   c.reduc.as<u32>(), c.reduced.as<K>()); GBSPH_COUNTED; }
-    { k_reduc_tail<<<1, 1, 0, s>>>(c.reduc.as<u32>(), &dsc->total, n); GBSPH_COUNTED; }
-    if (prof_tree >= 0) prof_end(c, prof_tree);
-    if ((e = sync_scalars(c)) != cudaSuccess) return e;
+    u8 *fa = c.flags_a.as<u8>(), *fb = c.flags_b.as<u8>();
+    u8 *fin = (level % 2 == 0) ? fa : fb;
+    // The radix sort is tried first when allowed; equal keys (whose order is the
+    // network's) send the build back to the bitonic sort, found at the sync below.
+    const bool radix = fast_sort && std::is_same<K, u32>::value;
+    for (int attempt = radix ? 0 : 1; attempt < 2; attempt++) {
+        {
+            ProfScope ps(c, kProfSort, P);
+            { k_morton<K><<<div_up(P, T), T, 0, s>>>(x, y, z, n, P, c.d_bbox.as<BBox>(), keys, vals); GBSPH_COUNTED; }
+            if (attempt == 0) {
+                if ((e = cudaMemsetAsync(&dsc->dup_keys, 0, sizeof(u32), s)) != cudaSuccess) return e;
+                if ((e = radix_sort_u32(c, (u32 *) keys, vals, n, s)) != cudaSuccess) return e;
+                { k_adjacent_dup<<<div_up(n, T), T, 0, s>>>((const u32 *) keys, n, &dsc->dup_keys); GBSPH_COUNTED; }
+            } else {
+                if ((e = bitonic_sort<K>(keys, vals, P, s)) != cudaSuccess) return e;
+            }
+        }
+        int prof_tree = c.prof.on ? prof_begin(c, kProfTree, n) : -1;
+        // leaf reduction: ping-pong split tables, final table is a for even levels
+        { k_split<K><<<div_up(n, T), T, 0, s>>>(keys, n, fa); GBSPH_COUNTED; }
+        for (u32 it = 1; it <= level; it++) {
+            if (it % 2 == 0) { k_reduce_iter<K><<<div_up(n, T), T, 0, s>>>(keys, n, fb, fa); GBSPH_COUNTED; }
+            else { k_reduce_iter<K><<<div_up(n, T), T, 0, s>>>(keys, n, fa, fb); GBSPH_COUNTED; }
+        }
+        if ((e = scan_exclusive_flags(fin, c.offsets.as<u32>(), n, &dsc->total, c.scan_scratch, s)) !=
+            cudaSuccess)
+            return e;
+        { k_compact_leaves<K><<<div_up(n, T), T, 0, s>>>(fin, c.offsets.as<u32>(), n, keys,
+                                                       c.reduc.as<u32>(), c.reduced.as<K>()); GBSPH_COUNTED; }
+        { k_reduc_tail<<<1, 1, 0, s>>>(c.reduc.as<u32>(), &dsc->total, n); GBSPH_COUNTED; }
+        if (prof_tree >= 0) prof_end(c, prof_tree);
+        if ((e = sync_scalars(c)) != cudaSuccess) return e;
+        if (attempt == 0 && !c.h_scalars->dup_keys) break;
+    }
     ProfScope ps_tree(c, kProfTree, 0);
     u32 L        = c.h_scalars->total;
     c.leaf_count = L;
@@ -530,13 +636,13 @@ cudaError_t bbox_from_merged(Ctx &c, u32 n) {
 }
 
 cudaError_t tree_build(Ctx &c, const f64 *x, const f64 *y, const f64 *z, const f64 *h, u32 n,
-                       u32 level, f64 htol, int key_bits, u32 morton_count) {
+                       u32 level, f64 htol, int key_bits, u32 morton_count, bool fast_sort) {
     if (key_bits == 64) {
         { k_bbox_fact<<<1, 32, 0, c.stream>>>(c.d_bbox.as<BBox>(), Morton<u64>::val_count); GBSPH_COUNTED; }
-        return tree_build_impl<u64>(c, x, y, z, h, n, level, htol, morton_count);
+        return tree_build_impl<u64>(c, x, y, z, h, n, level, htol, morton_count, false);
     }
     { k_bbox_fact<<<1, 32, 0, c.stream>>>(c.d_bbox.as<BBox>(), Morton<u32>::val_count); GBSPH_COUNTED; }
-    return tree_build_impl<u32>(c, x, y, z, h, n, level, htol, morton_count);
+    return tree_build_impl<u32>(c, x, y, z, h, n, level, htol, morton_count, fast_sort);
 }
 
 // explicit entry points for module-level exports (driver.cu)

@@ -203,3 +203,64 @@ def keplerian_disc(N, seed=12345, r_in=0.1, r_out=1.0, HoR=0.05, q=0.25, M=1.0, 
     return dict(pos=pos, vel=vel, h=h, u=u_int, pmass=pmass, gamma=5.0 / 3.0, cs0=cs0, q=q,
                 r0=1.0, M=M, G=G, periodic=False,
                 box_min=tuple(pos.min(0) - 1e-3), box_max=tuple(pos.max(0) + 1e-3))
+
+
+def _hcp_index_bounds(dr, bmin, bmax):
+    """Integer lattice bounds of LatticeHCP::get_box_index_bounds (shammath/crystalLattice.hpp:
+    145-170): coordinates divided by the lattice steps, truncated toward zero, widened by 1."""
+    steps = np.array([2.0, np.sqrt(3.0), 2 * np.sqrt(6.0) / 3])
+    cmin = (np.asarray(bmin, float) / steps) / dr
+    cmax = (np.asarray(bmax, float) / steps) / dr
+    return np.trunc(cmin).astype(np.int64) - 1, np.trunc(cmax).astype(np.int64) + 1
+
+
+def _hcp_points(dr, i, j, k):
+    """LatticeHCP::generator (crystalLattice.hpp:68-79)."""
+    return dr * np.stack([2 * i + (np.abs(j + k) % 2),
+                          np.sqrt(3.0) * (j + (1.0 / 3.0) * (np.abs(k) % 2)),
+                          2 * np.sqrt(6.0) * k / 3], 1)
+
+
+def homogeneous_box(n_target=1 << 25, bmin=(-0.6, -0.6, -0.6), bmax=(0.6, 0.6, 0.6), rho=1.0,
+                    u_inj=1.0):
+    """The reference's SPH throughput benchmark (examples/benchmarks/sph_homogeneous_benchmark.py):
+    an HCP lattice of about n_target particles filling the periodic box that the lattice
+    closes exactly (LatticeHCP::get_ideal_hcp_box), density rho, u = 0 except a central
+    injection u_inj W(r, 16 dr) (Model::add_kernel_value), h = dr as the lattice generator
+    sets it.  With n_target = 2^25 this gives 33,848,064 particles, the count of the
+    reference's published single-GPU runs."""
+    bmin = np.asarray(bmin, float)
+    bmax = np.asarray(bmax, float)
+    vol = float(np.prod(bmax - bmin))
+    dr = (0.74 * (vol / n_target) / ((4.0 / 3.0) * 3.1416)) ** (1.0 / 3.0)
+    # ideal periodic box (crystalLattice.hpp:172-202, 387-401)
+    cmin, cmax = _hcp_index_bounds(dr, bmin, bmax)
+    if cmax[0] - cmin[0] < 2:
+        cmax[0] += 1
+    if (cmax[1] + cmin[1]) % 2 != 0:
+        cmax[1] += 1
+    if (cmax[2] + cmin[2]) % 2 != 0:
+        cmax[2] += 1
+    lo = np.array([2.0 * cmin[0], np.sqrt(3.0) * cmin[1], 2 * np.sqrt(6.0) * cmin[2] / 3]) * dr
+    hi = np.array([2.0 * cmax[0], np.sqrt(3.0) * cmax[1], 2 * np.sqrt(6.0) * cmax[2] / 3]) * dr
+    # lattice sites inside [lo, hi) (GeneratorLatticeHCP.hpp:51-110, Patch.hpp:209-214)
+    gmin, gmax = _hcp_index_bounds(dr, lo, hi)
+    parts = []
+    ii = np.arange(gmin[0], gmax[0])
+    jj = np.arange(gmin[1], gmax[1])
+    for k in range(gmin[2], gmax[2]):
+        i, j = np.meshgrid(ii, jj, indexing="ij")
+        i, j = i.ravel(), j.ravel()
+        p = _hcp_points(dr, i, j, np.full_like(i, k))
+        keep = np.all((p >= lo) & (p < hi), axis=1)
+        parts.append(p[keep])
+    pos = np.concatenate(parts)
+    n = len(pos)
+    pmass = rho * float(np.prod(hi - lo)) / n
+    r = np.linalg.norm(pos, axis=1)
+    h_inj = 16 * dr
+    q = r / h_inj
+    f = np.where(q < 1, 0.25 * (2 - q) ** 3 - (1 - q) ** 3, np.where(q < 2, 0.25 * (2 - q) ** 3, 0.0))
+    u = u_inj * f / (np.pi * h_inj ** 3)
+    return dict(pos=pos, vel=np.zeros_like(pos), h=np.full(n, dr), u=u, pmass=pmass,
+                gamma=5.0 / 3.0, box_min=tuple(lo), box_max=tuple(hi), dr=dr)

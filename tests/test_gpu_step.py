@@ -72,6 +72,31 @@ def test_sedov_fp64_bitexact(n_cells, jitter, steps):
         compare_fields(model, sim)
 
 
+def test_duplicate_morton_keys_fp64_bitexact():
+    """Pairs of particles 1e-6 apart share their Morton cell: equal keys, whose order is
+    fixed by the bitonic network.  The step sorts with the radix sort first and must
+    notice the ties and fall back to the network (fifty tied pairs in the stable order
+    of the radix sort would not match the oracle's permutation by chance)."""
+    from shamrock_gb300 import setups
+
+    s = setups.sedov_taylor(8, jitter=0.05, seed=6)
+    rng = np.random.default_rng(6)
+    pick = rng.choice(len(s["h"]), 50, replace=False)
+    extra = s["pos"][pick] + 1e-6 * rng.standard_normal((50, 3))
+    s = dict(s)
+    s["pos"] = np.concatenate([s["pos"], extra])
+    s["vel"] = np.concatenate([s["vel"], s["vel"][pick]])
+    s["h"] = np.concatenate([s["h"], s["h"][pick]])
+    s["u"] = np.concatenate([s["u"], s["u"][pick]])
+    model, sim = make_pair(s)
+    for k in range(2):
+        lg = model.evolve_once()
+        lo = sim.evolve_once()
+        for key in KEYS_EXACT:
+            assert lg[key] == lo[key], (k, key)
+        compare_fields(model, sim)
+
+
 def test_clustered_free_boundary_fp64_bitexact():
     from shamrock_gb300 import setups
 
