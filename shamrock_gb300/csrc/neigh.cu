@@ -14,7 +14,9 @@
 // neighbours in exactly the reference order (ascending leaf, then in-leaf order).
 
 #include "gbsph_ctx.cuh"
+#include "split64.cuh"
 
+#include <cmath>
 #include <cstddef>
 #include <type_traits>
 
@@ -304,19 +306,31 @@ __global__ void k_rows(const u32 *__restrict__ sort_index, const u8 *__restrict_
 // largest); containment is decided in FP32 outside a rounding band, else in FP64.
 // leaf_thr (optional): per leaf, the FP32 bits (rounded up) of the largest pair-test
 // threshold thr_a = ((h_a htol)^2) R^2 over the rows it owns, 0 for a leaf owning none.
+// The exact containment test inside the FP32 band compares the doubles' ordered bit
+// patterns with integer operations (the FP64 pipe is scarce on GB300; particles lie on
+// their own leaf's faces, so the band is met often).
+__device__ __forceinline__ long long ord64(f64 v) {
+    long long b = __double_as_longlong(v);
+    if (b == (long long) 0x8000000000000000ull) b = 0; // -0 orders as +0
+    return b < 0 ? (b ^ 0x7fffffffffffffffll) : b;
+}
+
 __global__ void __launch_bounds__(128) k_owner(TreeView t, const NodeBoxF *__restrict__ fb,
                                                const NodePairF *__restrict__ rec,
                                                const u32 *__restrict__ row_rank, u32 n_rows,
                                                const f64 *__restrict__ sx, const f64 *__restrict__ sy,
                                                const f64 *__restrict__ sz, u32 *__restrict__ owner,
                                                u32 *__restrict__ flags, const f64 *__restrict__ sh,
-                                               f64 h_tol, u32 *__restrict__ leaf_thr) {
+                                               float h_tol_up, u32 *__restrict__ leaf_thr) {
     u32 row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n_rows) return;
     u32 r    = row_rank[row];
-    f64 p[3] = {sx[r], sy[r], sz[r]};
-    const float px = __double2float_rn(p[0]), py = __double2float_rn(p[1]),
-                pz = __double2float_rn(p[2]);
+    const f64 p[3] = {sx[r], sy[r], sz[r]};
+    const long long op[3] = {ord64(p[0]), ord64(p[1]), ord64(p[2])};
+    float px, py, pz, lo_unused;
+    split64(p[0], px, lo_unused);
+    split64(p[1], py, lo_unused);
+    split64(p[2], pz, lo_unused);
     const F8 fr = ldg256(&fb[0]);
     float M = fmaxf(fmaxf(fmaxf(fabsf(fr.a.x), fabsf(fr.a.y)), fmaxf(fabsf(fr.a.z), fabsf(fr.b.x))),
                     fmaxf(fabsf(fr.b.y), fabsf(fr.b.z)));
@@ -328,8 +342,8 @@ __global__ void __launch_bounds__(128) k_owner(TreeView t, const NodeBoxF *__res
         if (m < -band) return false;
         f64 l64[3], h64[3], rr;
         load_box(&t.boxes[node], l64, h64, rr);
-        return (l64[0] <= p[0]) && (p[0] <= h64[0]) && (l64[1] <= p[1]) && (p[1] <= h64[1])
-               && (l64[2] <= p[2]) && (p[2] <= h64[2]);
+        return (ord64(l64[0]) <= op[0]) && (op[0] <= ord64(h64[0])) && (ord64(l64[1]) <= op[1])
+               && (op[1] <= ord64(h64[1])) && (ord64(l64[2]) <= op[2]) && (op[2] <= ord64(h64[2]));
     };
     const u32 offn = t.off();
     u32 stack[kStack];
@@ -356,9 +370,11 @@ __global__ void __launch_bounds__(128) k_owner(TreeView t, const NodeBoxF *__res
         atomicOr(flags, kFlagOwnerMissing);
         found = 0;
     } else if (leaf_thr) {
-        f64 rint_a = __dmul_rn(sh[r], h_tol);
-        f64 thr_a  = __dmul_rn(__dmul_rn(rint_a, rint_a), kRkern * kRkern);
-        atomicMax(&leaf_thr[found], __float_as_uint(__double2float_ru(thr_a)));
+        // an FP32 upper bound of thr_a = fl64(fl64(h htol)^2 R^2): every factor rounded up
+        // (a float at or above a real number is at or above its nearest double)
+        const float rint = __fmul_ru(__double2float_ru(sh[r]), h_tol_up);
+        const float thr  = __fmul_ru(__fmul_ru(rint, rint), (float) (kRkern * kRkern));
+        atomicMax(&leaf_thr[found], __float_as_uint(thr));
     }
     owner[row] = found;
 }
@@ -511,6 +527,13 @@ __global__ void k_query(TreeView t, const f64 *__restrict__ qx, const f64 *__res
     if (!FILL) counts[q] = c;
 }
 
+// the smallest float at or above v (host)
+float up_f32(f64 v) {
+    float f = (float) v;
+    if ((f64) f < v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
 TreeView view(const Ctx &c) {
     return TreeView{c.lchild.as<u32>(), c.rchild.as<u32>(), c.lflag.as<u8>(), c.rflag.as<u8>(),
                     c.boxes.as<NodeBox>(), c.reduc.as<u32>(), c.leaf_count};
@@ -585,7 +608,7 @@ cudaError_t neigh_cache_build(Ctx &c, f64 h_tol, const float4 *P) {
         ProfScope ps(c, kProfOwner, n);
         { k_owner<<<div_up(n, 128), 128, 0, s>>>(t, fb, rec, c.row_rank.as<u32>(), n, c.sx.as<f64>(),
                                                c.sy.as<f64>(), c.sz.as<f64>(), c.owner.as<u32>(),
-                                               &dsc->flags, c.sh.as<f64>(), h_tol, leaf_thr); GBSPH_COUNTED; }
+                                               &dsc->flags, c.sh.as<f64>(), up_f32(h_tol), leaf_thr); GBSPH_COUNTED; }
     }
     auto stage1 = [&]() -> cudaError_t {
         cudaError_t err = c.leaf_ent.ensure(sizeof(uint2) * ((size_t) L * c.leaf_cap + 1), s);

@@ -524,36 +524,49 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
     const float vla[3] = {bf_hi(ha.b.z), bf_lo(ha.b.z), bf_hi(ha.b.w)};
     float sdiv = 0.f, sc[3] = {0.f, 0.f, 0.f};
     float R[3][3] = {}, Dv[3][3] = {}, Da[3][3] = {};
-    for (u32 k = k0; k < k1; k++) {
-        const u32 b   = rs.ent[k];
-        const F8 pb   = ldg256(&ms.P[2 * (size_t) b]);
-        const float r[3] = {(pa.a.x - pb.a.x) + (pa.b.x - pb.b.x), (pa.a.y - pb.a.y) + (pa.b.y - pb.b.y),
-                            (pa.a.z - pb.a.z) + (pa.b.z - pb.b.z)};
-        const float r2  = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
-        const float hib = pb.a.w;
-        if (r2 * hia2 > 4.f && r2 * (hib * hib) > 4.f) continue;
-        const F8 hb      = ldg256(&ms.H[2 * (size_t) b]);
-        const float4 ab  = __ldg(&A[b]);
-        const float rab  = sqrtf(r2);
-        const float v[3] = {(ha.a.x - hb.a.x) + (vla[0] - bf_hi(hb.b.z)),
-                            (ha.a.y - hb.a.y) + (vla[1] - bf_lo(hb.b.z)),
-                            (ha.a.z - hb.a.z) + (vla[2] - bf_hi(hb.b.w))};
-        const float w[3] = {aa.x - ab.x, aa.y - ab.y, aa.z - ab.z};
-        const float inv  = (rab < 1e-9f) ? 0.f : __frcp_rn(rab);
-        const float F    = k4a * m4_df32(rab * hia) * inv; // dW(r, h_a) / r
-        const float g[3] = {F * r[0], F * r[1], F * r[2]};
-        sdiv  = sdiv + ((v[0] * g[0] + v[1] * g[1]) + v[2] * g[2]);
-        sc[0] = sc[0] + (v[1] * g[2] - v[2] * g[1]);
-        sc[1] = sc[1] + (v[2] * g[0] - v[0] * g[2]);
-        sc[2] = sc[2] + (v[0] * g[1] - v[1] * g[0]);
+    // entries four at a time (pipeline rows are padded to 4), all records of the four
+    // neighbours requested together, the next four entries fetched behind them
+    uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, true, a) : make_uint4(a, a, a, a);
+    for (u32 k = k0; k < k1; k += 4) {
+        const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
+        F8 pb[4], hb[4];
+        float4 ab[4];
 #pragma unroll
-        for (int i = 0; i < 3; i++)
+        for (int q = 0; q < 4; q++) {
+            pb[q] = ldg256(&ms.P[2 * (size_t) bb[q]]);
+            hb[q] = ldg256(&ms.H[2 * (size_t) bb[q]]);
+            ab[q] = __ldg(&A[bb[q]]);
+        }
+        if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, true, a);
 #pragma unroll
-            for (int j = 0; j < 3; j++) {
-                R[i][j]  = R[i][j] - r[i] * g[j];
-                Dv[j][i] = Dv[j][i] - v[i] * g[j];
-                Da[j][i] = Da[j][i] - w[i] * g[j];
-            }
+        for (int q = 0; q < 4; q++) {
+            const float r[3] = {(pa.a.x - pb[q].a.x) + (pa.b.x - pb[q].b.x),
+                                (pa.a.y - pb[q].a.y) + (pa.b.y - pb[q].b.y),
+                                (pa.a.z - pb[q].a.z) + (pa.b.z - pb[q].b.z)};
+            const float r2  = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
+            const float hib = pb[q].a.w;
+            if (k + q >= k1 || (r2 * hia2 > 4.f && r2 * (hib * hib) > 4.f)) continue;
+            const float rab  = sqrtf(r2);
+            const float v[3] = {(ha.a.x - hb[q].a.x) + (vla[0] - bf_hi(hb[q].b.z)),
+                                (ha.a.y - hb[q].a.y) + (vla[1] - bf_lo(hb[q].b.z)),
+                                (ha.a.z - hb[q].a.z) + (vla[2] - bf_hi(hb[q].b.w))};
+            const float w[3] = {aa.x - ab[q].x, aa.y - ab[q].y, aa.z - ab[q].z};
+            const float inv  = (rab < 1e-9f) ? 0.f : __frcp_rn(rab);
+            const float F    = k4a * m4_df32(rab * hia) * inv; // dW(r, h_a) / r
+            const float g[3] = {F * r[0], F * r[1], F * r[2]};
+            sdiv  = sdiv + ((v[0] * g[0] + v[1] * g[1]) + v[2] * g[2]);
+            sc[0] = sc[0] + (v[1] * g[2] - v[2] * g[1]);
+            sc[1] = sc[1] + (v[2] * g[0] - v[0] * g[2]);
+            sc[2] = sc[2] + (v[0] * g[1] - v[1] * g[0]);
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    R[i][j]  = R[i][j] - r[i] * g[j];
+                    Dv[j][i] = Dv[j][i] - v[i] * g[j];
+                    Da[j][i] = Da[j][i] - w[i] * g[j];
+                }
+        }
     }
     const u32 i = rs.row_local[t];
     const float rho_a = mh3 * hia2 * hia;
