@@ -101,11 +101,14 @@ typedef struct {
     uint32_t ext_kind;
     double cs0, eos_r0, eos_q;
     double central_mass, constant_G;
-    /* Artificial viscosity: GBSPH_AV_CONSTANT (alpha_AV) or GBSPH_AV_VARYING_CD10,
+    /* Artificial viscosity: GBSPH_AV_CONSTANT (alpha_AV), GBSPH_AV_VARYING_CD10,
      * Cullen & Dehnen (2010): per-particle alpha relaxed towards a shock indicator built
      * from div v, curl v and d(div v)/dt, in [alpha_min, alpha_max] with decay rate
-     * sigma_decay (AVConfig::VaryingCD10, UpdateViscosity.cpp:122-215); alpha_u and
-     * beta_AV as for the constant form. */
+     * sigma_decay (AVConfig::VaryingCD10, UpdateViscosity.cpp:122-215), or
+     * GBSPH_AV_VARYING_MM97, Morris & Monaghan (1997): alpha driven by max(-div v, 0) and
+     * decaying to alpha_min (AVConfig::VaryingMM97, UpdateViscosity.cpp:53-118); alpha_u
+     * and beta_AV as for the constant form.  Both varying forms use the particle fields
+     * alpha_AV and soundspeed. */
     uint32_t av_kind;
     uint32_t pad2;
     double alpha_min, alpha_max, sigma_decay;
@@ -117,6 +120,7 @@ typedef struct {
 #define GBSPH_EXT_POINT_MASS 1
 #define GBSPH_AV_CONSTANT 0
 #define GBSPH_AV_VARYING_CD10 1
+#define GBSPH_AV_VARYING_MM97 2
 
 /* Synchronised solver state (the scheduler edges "time", "dt", "cfl_multiplier",
  * shammodels/sph/include/shammodels/sph/Solver.hpp:99-145). */

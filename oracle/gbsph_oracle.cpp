@@ -909,6 +909,23 @@ void cd10_update(u32 n, const f64 *divv, const f64 *curlv, const f64 *dtdivv, co
     }
 }
 
+// Morris & Monaghan (1997) switch, one implicit-Euler step towards alpha_min with the
+// source max(-div v, 0) (UpdateViscosity.cpp:53-118)
+void mm97_update(u32 n, const f64 *divv, const f64 *cs, const f64 *h, const f64 *alpha, f64 dt,
+                 f64 sigma_decay, f64 alpha_min, f64 alpha_max, f64 *alpha_new) {
+#pragma omp parallel for schedule(static)
+    for (i64 ii = 0; ii < (i64) n; ii++) {
+        const u32 i      = (u32) ii;
+        const f64 inv_tau = cs[i] * sigma_decay / h[i];
+        const f64 fact_t  = dt * inv_tau;
+        const f64 euler   = 1 / (1 + fact_t);
+        const f64 md      = -divv[i];
+        const f64 source  = (md > 0) ? md : f64(0);
+        const f64 na      = (alpha[i] + source * dt + fact_t * alpha_min) * euler;
+        alpha_new[i]      = (na < alpha_max) ? na : alpha_max;
+    }
+}
+
 // v_sig — shammodels/sph/src/Solver.cpp:2716-2788 (alpha_AV = 1, beta_AV = 2 fixed)
 void vsig_max(
     u32 n_local, const u32 *cnt, const u32 *scanned, const u32 *entries, const f64 *xyz,
@@ -1084,7 +1101,7 @@ struct Config {
     u32 ext_kind; // 0 none, 1 central point mass
     f64 cs0, eos_r0, eos_q;        // LP07: c_s^2 = cs0^2 (R^2 / r0^2)^(-q)
     f64 central_mass, constant_G;  // point mass at the origin
-    u32 av_kind;  // 0 constant, 1 varying CD10 (Cullen & Dehnen 2010)
+    u32 av_kind;  // 0 constant, 1 varying CD10 (Cullen & Dehnen 2010), 2 varying MM97
     u32 pad;
     f64 alpha_min, alpha_max, sigma_decay;
 };
@@ -1221,7 +1238,7 @@ void evolve_once(Sim &s, StepLog &log) {
         // velocities and the accelerations of the last evaluation, the switch update from
         // alpha_AV, then alpha on the ghosts
         std::vector<f64> alpha_upd, m_alpha;
-        if (cfg.av_kind == 1) {
+        if (cfg.av_kind == 1 || cfg.av_kind == 2) {
             std::vector<f64> m_a;
             merge_field(s, s.axyz, 3, m_a);
             s.divv.assign(n, 0);
@@ -1232,9 +1249,13 @@ void evolve_once(Sim &s, StepLog &log) {
                                m_h.data(), m_om.data(), cfg.pmass, s.divv.data(), s.curlv.data(),
                                s.dtdivv.data());
             alpha_upd.assign(n, 0);
-            cd10_update(n, s.divv.data(), s.curlv.data(), s.dtdivv.data(), s.soundspeed.data(),
-                        s.h.data(), s.alpha_AV.data(), dt, cfg.sigma_decay, cfg.alpha_min,
-                        cfg.alpha_max, alpha_upd.data());
+            if (cfg.av_kind == 1)
+                cd10_update(n, s.divv.data(), s.curlv.data(), s.dtdivv.data(), s.soundspeed.data(),
+                            s.h.data(), s.alpha_AV.data(), dt, cfg.sigma_decay, cfg.alpha_min,
+                            cfg.alpha_max, alpha_upd.data());
+            else
+                mm97_update(n, s.divv.data(), s.soundspeed.data(), s.h.data(), s.alpha_AV.data(), dt,
+                            cfg.sigma_decay, cfg.alpha_min, cfg.alpha_max, alpha_upd.data());
             merge_field(s, alpha_upd, 1, m_alpha);
         }
         s.P.assign(N, 0);
@@ -1249,7 +1270,7 @@ void evolve_once(Sim &s, StepLog &log) {
                        s.cache.part.entries.data(), mxyz.data(), m_v.data(), m_h.data(),
                        m_om.data(), m_u.data(), s.P.data(), s.cs.data(), cfg.pmass, cfg.alpha_u,
                        cfg.alpha_AV, cfg.beta_AV, s.axyz.data(), s.du.data(),
-                       cfg.av_kind == 1 ? m_alpha.data() : nullptr);
+                       cfg.av_kind != 0 ? m_alpha.data() : nullptr);
         if (cfg.ext_kind == 1)
             for (size_t k = 0; k < 3 * (size_t) n; k++) s.axyz[k] = s.axyz[k] + aext[k];
         f64 eps_v = leapfrog_correct(n, s.vxyz.data(), s.u.data(), s.axyz.data(), old_a.data(),
@@ -1260,7 +1281,7 @@ void evolve_once(Sim &s, StepLog &log) {
             s.cfl_mult = s.cfl_mult / 2;
         } else {
             rerun = false;
-            if (cfg.av_kind == 1) {
+            if (cfg.av_kind != 0) {
                 // write back (Solver.cpp:2620-2650, 3125-3160)
                 s.alpha_AV = alpha_upd;
                 s.soundspeed.assign(s.cs.begin(), s.cs.begin() + n);

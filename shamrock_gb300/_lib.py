@@ -20,6 +20,7 @@ GBSPH_FP64 = 0
 GBSPH_MIXED = 1
 GBSPH_AV_CONSTANT = 0
 GBSPH_AV_VARYING_CD10 = 1
+GBSPH_AV_VARYING_MM97 = 2
 
 _vp = C.c_void_p
 _u32 = C.c_uint32

@@ -587,9 +587,11 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
                 "unknown external force");
     REQUIRE_ARG(cfg->eos_kind != GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07 || cfg->eos_r0 > 0,
                 "locally isothermal EOS needs r0 > 0");
-    REQUIRE_ARG(cfg->av_kind == GBSPH_AV_CONSTANT || cfg->av_kind == GBSPH_AV_VARYING_CD10,
+    REQUIRE_ARG(cfg->av_kind == GBSPH_AV_CONSTANT || cfg->av_kind == GBSPH_AV_VARYING_CD10 ||
+                    cfg->av_kind == GBSPH_AV_VARYING_MM97,
                 "unknown artificial viscosity");
-    const bool cd10 = cfg->av_kind == GBSPH_AV_VARYING_CD10;
+    // varying viscosity (CD10 or MM97): per-particle alpha from the velocity gradients
+    const bool cd10 = cfg->av_kind != GBSPH_AV_CONSTANT;
     REQUIRE_ARG(!cd10 || (p->alpha_AV && p->soundspeed),
                 "the varying viscosity needs the alpha_AV and soundspeed fields");
     REQUIRE_ARG(!cd10 || !tape, "the adjoint step supports the constant viscosity only");
@@ -768,8 +770,12 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
                 CU(velgrad64(c, rs, hs, ar, ar + N, ar + 2 * (size_t) N, cfg->pmass, divv, cx, cy,
                              cz, cvs, dtdv));
             }
-            CU(cd10_update(c, n, divv, cx, cy, cz, cvs, dtdv, p->soundspeed, lf.h, p->alpha_AV,
-                           dt, cfg->sigma_decay, cfg->alpha_min, cfg->alpha_max, alpha_upd));
+            if (cfg->av_kind == GBSPH_AV_VARYING_CD10)
+                CU(cd10_update(c, n, divv, cx, cy, cz, cvs, dtdv, p->soundspeed, lf.h, p->alpha_AV,
+                               dt, cfg->sigma_decay, cfg->alpha_min, cfg->alpha_max, alpha_upd));
+            else
+                CU(mm97_update(c, n, divv, p->soundspeed, lf.h, p->alpha_AV, dt, cfg->sigma_decay,
+                               cfg->alpha_min, cfg->alpha_max, alpha_upd));
             if (mixed) {
                 CU(stage_alpha_mixed(c, N, n, alpha_upd));
             } else {

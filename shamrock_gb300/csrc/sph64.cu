@@ -531,6 +531,21 @@ __global__ void k_cd10(u32 n, const f64 *__restrict__ divv, const f64 *__restric
     alpha_new[i] = na;
 }
 
+// Morris & Monaghan (1997) switch (UpdateViscosity.cpp:53-118), comparisons as in the oracle
+__global__ void k_mm97(u32 n, const f64 *__restrict__ divv, const f64 *__restrict__ cs,
+                       const f64 *__restrict__ h, const f64 *__restrict__ alpha, f64 dt,
+                       f64 sigma_decay, f64 alpha_min, f64 alpha_max, f64 *__restrict__ alpha_new) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f64 inv_tau = cs[i] * sigma_decay / h[i];
+    const f64 fact_t  = dt * inv_tau;
+    const f64 euler   = 1 / (1 + fact_t);
+    const f64 md      = -divv[i];
+    const f64 source  = (md > 0) ? md : f64(0);
+    const f64 na      = (alpha[i] + source * dt + fact_t * alpha_min) * euler;
+    alpha_new[i]      = (na < alpha_max) ? na : alpha_max;
+}
+
 __global__ void k_gather_merged(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
                                 const u32 *__restrict__ ghost_src, const f64 *__restrict__ src,
                                 u32 stride, f64 *__restrict__ dst) {
@@ -705,6 +720,13 @@ cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64
     { k_cd10<<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cx, cy, cz, cvs, dtdivv, cs, h, alpha,
                                                   dt, sigma_decay, alpha_min, alpha_max,
                                                   alpha_new); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t mm97_update(Ctx &c, u32 n, const f64 *divv, const f64 *cs, const f64 *h,
+                        const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
+                        f64 *alpha_new) {
+    { k_mm97<<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cs, h, alpha, dt, sigma_decay, alpha_min,
+                                                  alpha_max, alpha_new); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t gather_merged64(Ctx &c, u32 N, u32 n_local, const f64 *src, u32 stride, f64 *dst) {

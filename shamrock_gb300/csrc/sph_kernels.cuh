@@ -92,6 +92,10 @@ cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64
                         const f64 *cz, u32 cvs, const f64 *dtdivv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
                         f64 *alpha_new);
+// the Morris & Monaghan (1997) switch update (UpdateViscosity.cpp:53-118)
+cudaError_t mm97_update(Ctx &c, u32 n, const f64 *divv, const f64 *cs, const f64 *h,
+                        const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
+                        f64 *alpha_new);
 // dst[r] = src[(merged id of rank r) -> local source] * stride, r < N (ghosts copy their source)
 cudaError_t gather_merged64(Ctx &c, u32 N, u32 n_local, const f64 *src, u32 stride, f64 *dst);
 // dst[row_local[t]] = src[row_rank[t]] for the n pipeline rows

@@ -56,9 +56,12 @@ class SolverConfig:
         self.av = dict(type="constant", alpha_u=float(alpha_u), alpha_AV=float(alpha_AV),
                        beta_AV=float(beta_AV))
 
-    def set_artif_viscosity_VaryingMM97(self, **kw):
-        raise NotImplementedError("the Morris & Monaghan (1997) switch is not on the GB300 path "
-                                  "(constant and VaryingCD10 are)")
+    def set_artif_viscosity_VaryingMM97(self, *, alpha_min, alpha_max, sigma_decay, alpha_u,
+                                        beta_AV):
+        """Morris & Monaghan (1997) switch (pySPHModel.cpp, UpdateViscosity.cpp:53-118)."""
+        self.av = dict(type="mm97", alpha_min=float(alpha_min), alpha_max=float(alpha_max),
+                       sigma_decay=float(sigma_decay), alpha_u=float(alpha_u),
+                       beta_AV=float(beta_AV), alpha_AV=0.0)
 
     def set_artif_viscosity_VaryingCD10(self, *, alpha_min, alpha_max, sigma_decay, alpha_u,
                                         beta_AV):
@@ -366,7 +369,7 @@ class Model:
         p.uint = d["uint"].data_ptr()
         p.duint = d["duint"].data_ptr()
         p.omega = d["omega"].data_ptr()
-        if self.cfg.av["type"] == "cd10":
+        if self.cfg.av["type"] in ("cd10", "mm97"):
             p.alpha_AV = d["alpha_AV"].data_ptr()
             p.soundspeed = d["soundspeed"].data_ptr()
             p.divv = d["divv"].data_ptr()
@@ -400,8 +403,8 @@ class Model:
             s.constant_G = c.constant_G
         s.pmass = c.gpart_mass
         s.alpha_u, s.alpha_AV, s.beta_AV = c.av["alpha_u"], c.av["alpha_AV"], c.av["beta_AV"]
-        if c.av["type"] == "cd10":
-            s.av_kind = L.GBSPH_AV_VARYING_CD10
+        if c.av["type"] in ("cd10", "mm97"):
+            s.av_kind = L.GBSPH_AV_VARYING_CD10 if c.av["type"] == "cd10" else L.GBSPH_AV_VARYING_MM97
             s.alpha_min, s.alpha_max = c.av["alpha_min"], c.av["alpha_max"]
             s.sigma_decay = c.av["sigma_decay"]
         s.cfl_cour, s.cfl_force = c.cfl_cour, c.cfl_force

@@ -1,4 +1,5 @@
-"""Varying artificial viscosity (Cullen & Dehnen 2010) on the GPU against the oracle.
+"""Varying artificial viscosity on the GPU against the oracle: the Cullen & Dehnen (2010)
+switch and the Morris & Monaghan (1997) one.
 
 FP64: every particle field, alpha_AV, the stored sound speed and the diagnostics div v,
 curl v, d(div v)/dt are bit-identical to the oracle after each step, with the step
@@ -27,13 +28,16 @@ def _setup(n_cells=8, jitter=0.05, seed=3):
     return s
 
 
-def make_pair(s, precision="fp64", alpha0=0.1, cs0=0.0):
+def make_pair(s, precision="fp64", alpha0=0.1, cs0=0.0, av="cd10"):
     import shamrock_gb300 as sg
 
     ctx = sg.Context()
     model = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
     cfg = model.gen_default_config()
-    cfg.set_artif_viscosity_VaryingCD10(**CD10)
+    if av == "cd10":
+        cfg.set_artif_viscosity_VaryingCD10(**CD10)
+    else:
+        cfg.set_artif_viscosity_VaryingMM97(**CD10)
     cfg.set_boundary_periodic()
     cfg.set_eos_adiabatic(s["gamma"])
     cfg.set_particle_mass(s["pmass"])
@@ -49,7 +53,8 @@ def make_pair(s, precision="fp64", alpha0=0.1, cs0=0.0):
     oc = O.OrcConfig(gamma=s["gamma"], pmass=s["pmass"], alpha_u=1.0, alpha_AV=0.0, beta_AV=2.0,
                      cfl_cour=0.3, cfl_force=0.3, cfl_mult_stiffness=2.0, htol_up_coarse=1.1,
                      htol_up_fine=1.1, epsilon_h=1e-6, h_iter_per_subcycles=50,
-                     h_max_subcycles=100, tree_reduction_level=3, periodic=1, av_kind=1,
+                     h_max_subcycles=100, tree_reduction_level=3, periodic=1,
+                     av_kind=1 if av == "cd10" else 2,
                      alpha_min=CD10["alpha_min"], alpha_max=CD10["alpha_max"],
                      sigma_decay=CD10["sigma_decay"])
     oc.bmin[:] = list(s["box_min"])
@@ -63,10 +68,10 @@ KEYS_EXACT = ("n_ghost", "leaf_count", "cache_size", "h_subcycles", "h_iteration
               "corrector_iters", "next_dt", "cfl_mult")
 
 
-@pytest.mark.parametrize("cs0", [0.0, 0.5])
-def test_cd10_fp64_bitexact(cs0):
+@pytest.mark.parametrize("av,cs0", [("cd10", 0.0), ("cd10", 0.5), ("mm97", 0.5)])
+def test_varying_av_fp64_bitexact(av, cs0):
     s = _setup()
-    model, sim = make_pair(s, cs0=cs0)
+    model, sim = make_pair(s, cs0=cs0, av=av)
     moved = False
     for k in range(4):
         lg = model.evolve_once()
@@ -77,20 +82,21 @@ def test_cd10_fp64_bitexact(cs0):
         o = sim.get()
         for key in ("xyz", "vxyz", "axyz", "hpart", "uint", "duint", "omega"):
             assert np.array_equal(g[key], o[key]), (k, key)
-        av = sim.get_av()
+        oav = sim.get_av()
         for key in ("alpha_AV", "soundspeed", "divv", "curlv", "dtdivv"):
-            assert np.array_equal(g[key], av[key]), (k, key)
+            assert np.array_equal(g[key], oav[key]), (k, key)
         moved |= bool(np.any(g["alpha_AV"] != 0.1))
     assert moved  # the switch did act
 
 
-def test_cd10_mixed_vs_fp64():
+@pytest.mark.parametrize("av", ["cd10", "mm97"])
+def test_varying_av_mixed_vs_fp64(av):
     """One step from the same state: accelerations, du/dt and the updated alpha of the
     mixed path against FP64 (normalised by the largest magnitude of each field)."""
     s = _setup(n_cells=10, jitter=0.05, seed=5)
     res = {}
     for prec in ("fp64", "mixed"):
-        m, _ = make_pair(s, precision=prec, cs0=0.3)
+        m, _ = make_pair(s, precision=prec, cs0=0.3, av=av)
         m.evolve_once()
         res[prec] = m.collect_data()
     a, b = res["mixed"], res["fp64"]

@@ -100,3 +100,25 @@ def test_cd10_update_closed_form():
     new = np.where(loc > before["alpha_AV"], loc, new)
     assert dt > 0 and np.all(np.isfinite(h_b))
     assert np.allclose(av["alpha_AV"], new, rtol=1e-12, atol=1e-15)
+
+
+def test_mm97_update_closed_form():
+    """The Morris & Monaghan (1997) update against its closed form."""
+    pos, h = _lattice(8, 0.2, 9)
+    n = len(h)
+    rng = np.random.default_rng(13)
+    vel = 0.05 * rng.standard_normal((n, 3))
+    cfg = _cfg(1.0 / n, (0, 0, 0), (1, 1, 1), 1)
+    cfg.av_kind = 2
+    sim = O.Sim(cfg, pos, vel, h, np.full(n, 1.0))
+    sim.set_av(alpha=np.full(n, 0.2), soundspeed=np.full(n, 0.7))
+    sim.evolve_once()
+    before = sim.get_av()
+    _, dt, _ = sim.get_time()
+    sim.evolve_once()
+    av = sim.get_av()
+    hh = sim.get()["hpart"]
+    fact = dt * before["soundspeed"] * 0.1 / hh
+    new = (before["alpha_AV"] + np.maximum(-av["divv"], 0) * dt + fact * 0.0) / (1 + fact)
+    assert dt > 0
+    assert np.allclose(av["alpha_AV"], np.minimum(new, 1.0), rtol=1e-12, atol=1e-15)
