@@ -307,6 +307,13 @@ int gbsph_kdk_correct(gbsph_ctx *ctx, const gbsph_particles *p, gbsph_vec3 a_old
 int gbsph_cfl(gbsph_ctx *ctx, const double *h, const double *vsig, gbsph_vec3 a, uint32_t n,
               double C_cour, double C_force, double *dt_part, double *dt_min_host, void *stream);
 
+/* Conservation totals of ConservativeCheck::check_conservation
+ * (shammodels/sph/src/modules/ConservativeCheck.cpp:56-180), in FP64 with a fixed
+ * summation order: out_host = {sum m v (3), sum m a (3), sum m (u + v.v / 2),
+ * sum m (v.a + du)}, with a the caller's total acceleration (hydro + external). */
+int gbsph_conservation(gbsph_ctx *ctx, const gbsph_particles *p, double pmass, double out_host[8],
+                       void *stream);
+
 /* ------------------------------------------------------------------ full step */
 
 /* One Solver::evolve_once on one patch (shammodels/sph/src/Solver.cpp:1942-3272):

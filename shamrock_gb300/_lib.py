@@ -117,6 +117,7 @@ SIGNATURES = {
     "gbsph_profile_name": (C.c_char_p, [_u32]),
     "gbsph_profile_enable": (C.c_int, [_vp, C.c_int]),
     "gbsph_profile_read": (C.c_int, [_vp, _vp, _vp, _vp, _u32]),
+    "gbsph_conservation": (C.c_int, [_vp, _P(Particles), _f64, _P(_f64), _vp]),
 }
 
 _lib = None

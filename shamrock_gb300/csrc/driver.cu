@@ -501,6 +501,23 @@ int gbsph_cfl(gbsph_ctx *ctx, const double *h, const double *vsig, gbsph_vec3 a,
     return GBSPH_OK;
 }
 
+int gbsph_conservation(gbsph_ctx *ctx, const gbsph_particles *p, double pmass, double out_host[8],
+                       void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(p && out_host, "null argument");
+    REQUIRE_ARG(p->n > 0, "empty patch");
+    REQUIRE_ARG(p->vxyz.stride == p->axyz.stride, "vxyz and axyz must share one element stride");
+    LocalFields lf{p->xyz.x,  p->xyz.y,  p->xyz.z,  p->vxyz.x, p->vxyz.y,  p->vxyz.z,
+                   p->axyz.x, p->axyz.y, p->axyz.z, p->vxyz.stride, p->hpart, p->uint, p->duint};
+    CU(c.av_diag.ensure(sizeof(f64) * (8 * 1024 + 8), c.stream));
+    f64 *scratch = c.av_diag.as<f64>();
+    CU(conservation64(c, lf, p->n, pmass, scratch + 8 * 1024, scratch));
+    CU(cudaMemcpyAsync(out_host, scratch + 8 * 1024, 8 * sizeof(f64), cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
+    return GBSPH_OK;
+}
+
 int gbsph_eos_locally_isothermal(gbsph_ctx *ctx, gbsph_vec3 xyz, const double *h, uint32_t n,
                                  double pmass, double cs0, double r0, double q, double *P,
                                  double *cs, void *stream) {

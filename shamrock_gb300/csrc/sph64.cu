@@ -410,6 +410,52 @@ __global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f
     lf.u[i]   = u;
 }
 
+// ---------------------------------------------------------------- conservation totals
+// ConservativeCheck::check_conservation (shammodels/sph/src/modules/ConservativeCheck.cpp:
+// 56-180): sum v, sum a, sum (u + v.v / 2) and sum (v.a + du), each times the particle
+// mass, in FP64.  Per-block partial sums in a fixed tree order, then one block adds the
+// partials in block order: the totals are the same from run to run.
+constexpr u32 kConsBlock = 256;
+
+__global__ void __launch_bounds__(kConsBlock) k_cons_partial(LocalFields lf, u32 n,
+                                                            f64 *__restrict__ part) {
+    __shared__ f64 sm[8][kConsBlock];
+    const u32 t = threadIdx.x;
+    f64 v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (u32 i = blockIdx.x * kConsBlock + t; i < n; i += gridDim.x * kConsBlock) {
+        const size_t iv = (size_t) i * lf.vs;
+        const f64 vx = lf.vx[iv], vy = lf.vy[iv], vz = lf.vz[iv];
+        const f64 ax = lf.ax[iv], ay = lf.ay[iv], az = lf.az[iv];
+        v[0] += vx;
+        v[1] += vy;
+        v[2] += vz;
+        v[3] += ax;
+        v[4] += ay;
+        v[5] += az;
+        v[6] += lf.u[i] + 0.5 * ((vx * vx + vy * vy) + vz * vz);
+        v[7] += ((vx * ax + vy * ay) + vz * az) + lf.du[i];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) sm[k][t] = v[k];
+    __syncthreads();
+    for (u32 s = kConsBlock / 2; s > 0; s >>= 1) {
+        if (t < s)
+#pragma unroll
+            for (int k = 0; k < 8; k++) sm[k][t] += sm[k][t + s];
+        __syncthreads();
+    }
+    if (t < 8) part[(size_t) blockIdx.x * 8 + t] = sm[t][0];
+}
+
+__global__ void k_cons_final(const f64 *__restrict__ part, u32 nb, f64 pmass,
+                             f64 *__restrict__ out) {
+    const u32 k = threadIdx.x;
+    if (k >= 8) return;
+    f64 s = 0;
+    for (u32 b = 0; b < nb; b++) s += part[(size_t) b * 8 + k];
+    out[k] = pmass * s;
+}
+
 // ---------------------------------------------------------------- varying AV (CD10)
 // div v and curl v (DiffOperator.cpp:95-140, 200-245) and d(div v)/dt from the linearly
 // corrected gradients (DiffOperatorDtDivv.cpp:116-210) in one pass over the row; each
@@ -727,6 +773,13 @@ cudaError_t mm97_update(Ctx &c, u32 n, const f64 *divv, const f64 *cs, const f64
                         f64 *alpha_new) {
     { k_mm97<<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cs, h, alpha, dt, sigma_decay, alpha_min,
                                                   alpha_max, alpha_new); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+cudaError_t conservation64(Ctx &c, const LocalFields &lf, u32 n, f64 pmass, f64 *out_dev,
+                           f64 *scratch) {
+    const u32 nb = 1024;
+    { k_cons_partial<<<nb, kConsBlock, 0, c.stream>>>(lf, n, scratch); GBSPH_COUNTED; }
+    { k_cons_final<<<1, 32, 0, c.stream>>>(scratch, nb, pmass, out_dev); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t gather_merged64(Ctx &c, u32 N, u32 n_local, const f64 *src, u32 stride, f64 *dst) {

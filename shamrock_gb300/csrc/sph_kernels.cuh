@@ -92,6 +92,10 @@ cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64
                         const f64 *cz, u32 cvs, const f64 *dtdivv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
                         f64 *alpha_new);
+// conservation totals {sum m v (3), sum m a (3), sum m (u + v.v/2), sum m (v.a + du)} of
+// n local particles into out_dev[8] (scratch: 8 x 1024 doubles), deterministic order
+cudaError_t conservation64(Ctx &c, const LocalFields &lf, u32 n, f64 pmass, f64 *out_dev,
+                           f64 *scratch);
 // the Morris & Monaghan (1997) switch update (UpdateViscosity.cpp:53-118)
 cudaError_t mm97_update(Ctx &c, u32 n, const f64 *divv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,

@@ -442,6 +442,18 @@ class Model:
     def timestep(self):
         return self.evolve_once()
 
+    def conservation_totals(self):
+        """FP64 totals of the reference's ConservativeCheck: momentum sum m v, force sum
+        m a, energy sum m (u + v^2/2) and its rate sum m (v.a + du/dt)."""
+        import ctypes as C
+
+        lib = self._lib()
+        p = self._particles_struct()
+        out = (C.c_double * 8)()
+        lib.check(lib.lib.gbsph_conservation(lib.handle, C.byref(p), self.cfg.gpart_mass, out, None))
+        return dict(momentum=np.array(out[0:3]), force=np.array(out[3:6]), energy=out[6],
+                    energy_rate=out[7])
+
     def evolve_once_override_time(self, t_current, dt_input):
         self.time = float(t_current)
         self.dt = float(dt_input)

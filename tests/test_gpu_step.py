@@ -97,6 +97,29 @@ def test_duplicate_morton_keys_fp64_bitexact():
         compare_fields(model, sim)
 
 
+def test_conservation_totals():
+    """gbsph_conservation (the reference's ConservativeCheck sums) against numpy sums of
+    the same fields: FP64, agreement to summation-order round-off."""
+    from shamrock_gb300 import setups
+
+    s = setups.sedov_taylor(8, jitter=0.05, seed=2)
+    model, _ = make_pair(s)
+    for _ in range(2):
+        model.evolve_once()
+    tot = model.conservation_totals()
+    d = model.collect_data()
+    m = s["pmass"]
+    v, a = d["vxyz"], d["axyz"]
+    scale_v = m * np.abs(v).sum()
+    scale_a = m * np.abs(a).sum()
+    assert np.allclose(tot["momentum"], m * v.sum(0), rtol=0, atol=1e-12 * scale_v)
+    assert np.allclose(tot["force"], m * a.sum(0), rtol=0, atol=1e-12 * scale_a)
+    e = m * np.sum(d["uint"] + 0.5 * np.sum(v * v, 1))
+    de = m * np.sum(np.sum(v * a, 1) + d["duint"])
+    assert abs(tot["energy"] - e) <= 1e-12 * abs(e)
+    assert abs(tot["energy_rate"] - de) <= 1e-10 * (m * np.sum(np.abs(np.sum(v * a, 1)) + np.abs(d["duint"])))
+
+
 def test_clustered_free_boundary_fp64_bitexact():
     from shamrock_gb300 import setups
 
