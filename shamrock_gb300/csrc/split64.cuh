@@ -10,7 +10,8 @@
 // where hi, lo and the scale 2^(E - 52) are normal floats, so the results equal
 // __double2float_rn(v) and __double2float_rn(v - (double) hi) bit for bit.  Other values
 // (0, tiny, huge, inf, nan) take the FP64 route, so the function is exact everywhere.
-// Header-only and free of CUDA intrinsics so the same code is checked on the host.
+// Header-only and free of CUDA intrinsics so the same code is checked on the host
+// (tests/native/split64_check.cpp).
 #pragma once
 
 #include <cstdint>
