@@ -5,7 +5,8 @@ reference (shammodels/sph/src/pySPHModel.cpp: get_Model_SPH :1725-1754, the
 SolverConfig setters :107-262, model methods :773-1433), so that scripts written
 for ``shamrock.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")``
 run unchanged on the subset the GB300 path covers: one patch, periodic or free
-box, M4 kernel, constant artificial viscosity, adiabatic EOS.
+box, M4 kernel, constant or varying (CD10, MM97) artificial viscosity, adiabatic or
+locally isothermal EOS, a central point mass, Phantom dump I/O.
 
 Particle fields live on the GPU as float64 torch tensors in structure-of-arrays
 layout; every step runs through the C ABI (``libgbsph.so``).  Setup helpers work
@@ -25,6 +26,22 @@ FIELDS_SCAL = ("hpart", "uint", "duint")
 # divv, curlv, dtdivv (the reference adds them to the layout for that AV only)
 FIELDS_AV_SCAL = ("alpha_AV", "soundspeed", "divv", "dtdivv")
 FIELDS_AV_VEC = ("curlv",)
+# the gravitational constant in SI (shamunits/Constants.hpp:130)
+G_SI = 6.6743015e-11
+
+
+class UnitSystem:
+    """shamrock.UnitSystem (shamunits/UnitSystem.hpp:148-160, pyUnits.cpp:30-55): the SI
+    value of one code unit of time, length and mass."""
+
+    def __init__(self, unit_time=1.0, unit_length=1.0, unit_mass=1.0):
+        self.unit_time = float(unit_time)
+        self.unit_length = float(unit_length)
+        self.unit_mass = float(unit_mass)
+
+    def constant_G(self):
+        """G in code units: G_SI M T^2 / L^3."""
+        return G_SI * self.unit_mass * self.unit_time**2 / self.unit_length**3
 
 
 class SolverConfig:
@@ -49,7 +66,8 @@ class SolverConfig:
         self.precision = "fp64"
         self.ext_forces = []
         # G without a unit system is the SI value, as the reference's get_constant_G
-        self.constant_G = 6.6743e-11
+        self.constant_G = G_SI
+        self.units = None
 
     # -- setters named as the reference's python bindings
     def set_artif_viscosity_Constant(self, alpha_u, alpha_AV, beta_AV):
@@ -95,6 +113,11 @@ class SolverConfig:
         from the unit system, SI without one)."""
         self.constant_G = float(G)
 
+    def set_units(self, units):
+        """SolverConfig::set_units: the code's unit system; G follows it."""
+        self.units = units
+        self.constant_G = units.constant_G()
+
     def set_particle_mass(self, pmass):
         self.gpart_mass = float(pmass)
 
@@ -132,8 +155,14 @@ class SolverConfig:
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
 
+    def has_field_alphaAV(self):
+        return self.av["type"] in ("cd10", "mm97")
+
     def to_dict(self):
-        return dict(self.__dict__)
+        d = dict(self.__dict__)
+        if self.units is not None:
+            d["units"] = dict(self.units.__dict__)
+        return d
 
     def print_status(self):
         print(json.dumps(self.to_dict(), indent=1))
@@ -511,3 +540,122 @@ class Model:
     def get_thermal_energy(self):
         d = self._to_device()
         return float(self.cfg.gpart_mass * d["uint"].sum().item())
+
+    # ------------------------------------------------------------------ Phantom dumps
+    def gen_config_from_phantom_dump(self, dump, bypass_error=False):
+        """Model::gen_config_from_phantom_dump (Model.cpp:1203-1222): particle mass from
+        massoftype[0], C_cour and C_force, the EOS of the dump's ieos, the varying CD10
+        viscosity (alpha in [0, 1], sigma 0.1, the dump's alphau, beta 2), the dump's
+        units, periodic boundaries when the header holds a box (xmin) and free ones
+        otherwise."""
+        from . import phantom as P
+
+        cfg = SolverConfig()
+        cfg.gpart_mass = dump.read_header_floats("massoftype")[0]
+        cfg.cfl_cour = dump.read_header_float("C_cour")
+        cfg.cfl_force = dump.read_header_float("C_force")
+        cfg.eos = P.eos_config_from_dump(dump, bypass_error)
+        cfg.set_artif_viscosity_VaryingCD10(alpha_min=0.0, alpha_max=1.0, sigma_decay=0.1,
+                                            alpha_u=dump.read_header_float("alphau"), beta_AV=2.0)
+        cfg.set_units(UnitSystem(unit_time=dump.read_header_float("utime"),
+                                 unit_length=dump.read_header_float("udist"),
+                                 unit_mass=dump.read_header_float("umass")))
+        cfg.boundary = "periodic" if dump.has_header_entry("xmin") else "free"
+        return cfg
+
+    def init_from_phantom_dump(self, dump, hpart_fact_load=1.0):
+        """Model::init_from_phantom_dump (Model.cpp:1225-1429) for one patch: the box from
+        the header's xmin..zmax, else the particles' bounding box grown 1.2 times about its
+        centre; the gas particles of block 0 inside the box with h >= 0 (Phantom marks
+        accreted or dead particles with h < 0), in file order, h scaled by
+        hpart_fact_load; u and alpha_AV when the dump holds them; the dump's time.  Sink
+        particles (block 1) are not on the GB300 path: a dump holding any raises."""
+        b0 = dump.blocks[0]
+        x, y, z = (b0.fill_vec(k) for k in ("x", "y", "z"))
+        if dump.has_header_entry("xmin"):
+            bmin = np.array([dump.read_header_float(k) for k in ("xmin", "ymin", "zmin")])
+            bmax = np.array([dump.read_header_float(k) for k in ("xmax", "ymax", "zmax")])
+        else:
+            lo = np.array([x.min(), y.min(), z.min()])
+            hi = np.array([x.max(), y.max(), z.max()])
+            center = (lo + hi) * 0.5
+            d = (hi - lo) * 0.5 * 1.2
+            bmin, bmax = center - d, center + d
+        self.resize_simulation_box(bmin, bmax)
+        if len(dump.blocks) > 1 and dump.blocks[1].tot_count > 0:
+            raise NotImplementedError("sink particles are not on the GB300 path")
+        h = b0.fill_vec("h")
+        v = np.stack([b0.fill_vec(k) for k in ("vx", "vy", "vz")], 1)
+        u = b0.fill_vec("u")
+        alpha = b0.fill_vec("alpha")
+        self.set_time(dump.read_header_float("time"))
+        pos = np.stack([x, y, z], 1)
+        keep = np.all((pos >= self.box_min) & (pos < self.box_max), axis=1) & (h >= 0)
+        if v.size == 0:
+            v = np.zeros((x.size, 3))
+        self.set_particles(pos[keep], v[keep], h[keep] * hpart_fact_load,
+                           u[keep] if u.size else None,
+                           alpha=alpha[keep] if alpha.size else None)
+
+    def make_phantom_dump(self):
+        """Model::make_phantom_dump (Model.cpp:1491-1621): the header Phantom needs to
+        restart (counts, EOS, time, dt, CFL, massoftype, the box when periodic, units)
+        and block 0 with x, y, z, vx, vy, vz, u (real*8) and h, plus alpha and divv with a
+        varying viscosity (real*4).
+
+        Written as the reference writes them except ymax and zmax, which hold the box's
+        upper y and z bounds (the reference stores its upper x bound in both, correct for
+        cubic boxes only)."""
+        from . import phantom as P
+
+        c = self.cfg
+        d = self.collect_data()
+        n = int(d["hpart"].shape[0])
+        dump = P.PhantomDump()
+        dump.override_magic_number()
+        dump.iversion = 1
+        dump.fileid = f"{'FT:Phantom Shamrock writer':100s}"
+        fi, i64, i32, fr, f64 = (dump.table_header_fort_int, dump.table_header_i64,
+                                 dump.table_header_i32, dump.table_header_fort_real,
+                                 dump.table_header_f64)
+        for t in (fi, i64):
+            t.add("nparttot", n)
+            t.add("ntypes", 8)
+            t.add("npartoftype", n)
+            for _ in range(7):
+                t.add("npartoftype", 0)
+        for k, v in (("nblocks", 1), ("nptmass", 0), ("ndustlarge", 0), ("ndustsmall", 0),
+                     ("idust", 7), ("idtmax_n", 1), ("idtmax_frac", 0), ("idumpfile", 0),
+                     ("majorv", 2023), ("minorv", 0), ("microv", 0), ("isink", 0)):
+            fi.add(k, v)
+        i32.add("iexternalforce", 0)
+        P.write_eos_in_dump(c.eos, dump)
+        for k, v in (("time", self.time), ("dtmax", self.dt), ("rhozero", 0.0),
+                     ("hfact", self.get_hfact()), ("tolh", 0.0001), ("C_cour", c.cfl_cour),
+                     ("C_force", c.cfl_force), ("alpha", 0.0), ("alphau", 1.0), ("alphaB", 1.0)):
+            fr.add(k, v)
+        fr.add("massoftype", c.gpart_mass)
+        for _ in range(7):
+            fr.add("massoftype", 0.0)
+        for k in ("Bextx", "Bexty", "Bextz", "dum"):
+            fr.add(k, 0.0)
+        if c.boundary == "periodic":
+            for ax, k in enumerate("xyz"):
+                fr.add(k + "min", float(self.box_min[ax]))
+                fr.add(k + "max", float(self.box_max[ax]))
+        for k, v in (("get_conserv", -1.0), ("etot_in", 0.59762), ("angtot_in", 0.0189694),
+                     ("totmom_in", 0.0306284)):
+            fr.add(k, v)
+        P.write_units_in_dump(c.units, dump)
+        blk = P.PhantomDumpBlock(n)
+        for ax, k in enumerate("xyz"):
+            blk.set_array("fort_real", k, d["xyz"][:, ax])
+        blk.set_array("f32", "h", d["hpart"])
+        if c.has_field_alphaAV():
+            blk.set_array("f32", "alpha", d["alpha_AV"])
+            blk.set_array("f32", "divv", d["divv"])
+        for ax, k in enumerate(("vx", "vy", "vz")):
+            blk.set_array("fort_real", k, d["vxyz"][:, ax])
+        blk.set_array("fort_real", "u", d["uint"])
+        dump.blocks.append(blk)
+        return dump

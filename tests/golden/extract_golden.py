@@ -15,6 +15,9 @@ Fixtures produced (source files inside the Shamrock tree):
 - karras_radix_tree_aabb.json src/tests/shamtree/KarrasRadixTreeAABBTests.cpp
 - clbvh_object_iterator.json src/tests/shamtree/CLBVHObjectIteratorTests.cpp
 - h_iteration.json           src/tests/shammodels/sph/modules/IterateSmoothingLengthDensityTests.cpp
+- sedov_taylor_table.json    src/shamphys/src/sedov_soluce_arrays.hpp (every 15th point of the
+                             reference's tabulated Sedov-Taylor solution, plus the points
+                             either side of the shock)
 """
 
 import json
@@ -126,5 +129,29 @@ def extract(ref_root):
         print("wrote", out_name, "tests:", list(fixture["tests"]))
 
 
+def extract_sedov(ref_root):
+    """Subsample of the reference's Sedov-Taylor table (gamma 5/3, E = 1, rho0 = 1, t = 0.1)."""
+    path = os.path.join(ref_root, "src", "shamphys", "src", "sedov_soluce_arrays.hpp")
+    with open(path) as f:
+        src = _strip_comments(f.read())
+    cols = {}
+    for name in ("r_theo", "vr_theo", "rho_theo", "p_theo"):
+        m = re.search(r"double\s+" + name + r"\[\]\s*=\s*\{(.*?)\};", src, re.S)
+        cols[name] = [float(t) for t in m.group(1).replace("\n", " ").split(",") if t.strip()]
+    n = len(cols["r_theo"])
+    jump = max(range(1, n), key=lambda i: abs(cols["rho_theo"][i] - cols["rho_theo"][i - 1]))
+    keep = sorted(set(range(0, n, 15)) | set(range(max(jump - 3, 0), min(jump + 3, n))) | {n - 1})
+    fixture = {"source": "src/shamphys/src/sedov_soluce_arrays.hpp", "count_in_source": n,
+               "case": {"gamma": 5.0 / 3.0, "e_blast": 1.0, "rho0": 1.0, "t": 0.1},
+               "index": keep}
+    for name, vals in cols.items():
+        fixture[name] = [vals[i] for i in keep]
+    with open(os.path.join(HERE, "sedov_taylor_table.json"), "w") as f:
+        json.dump(fixture, f, indent=0)
+    print("wrote sedov_taylor_table.json points:", len(keep))
+
+
 if __name__ == "__main__":
-    extract(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    extract(root)
+    extract_sedov(root)

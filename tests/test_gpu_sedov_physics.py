@@ -1,11 +1,16 @@
 """Physics check of the whole step on the GPU: the Sedov-Taylor blast against the
-self-similar solution, and energy conservation through the FP64 conservation totals.
+self-similar solution (shamrock_gb300.sedov, the closed form pinned to the reference's
+table in shamphys/src/SedovTaylor.cpp), and energy conservation through the FP64
+conservation totals.
 
-The strong-shock radius of a point explosion of energy E in a uniform medium of density
-rho is R(t) = xi0 (E t^2 / rho)^(1/5), xi0 = 1.1517 for gamma = 5/3 (Sedov 1959; the
-reference compares its runs with the same solution, shamphys/src/SedovTaylor.cpp).  SPH
-spreads the shock over a couple of smoothing lengths, so the radius of the density peak is
-checked to 10 %."""
+At 32,000 particles SPH spreads the shock over a couple of smoothing lengths and the
+viscosity turns some kinetic energy into heat, so the checks are on what that smoothing
+leaves alone: the radii of the density and velocity peaks and the peak velocity (10 %),
+the total radial momentum (10 %) and the kinetic share of the blast energy (25 %).  The
+FP64 oracle run of the same set-up (CPU, 110 steps) gives: density peak 0.345 against
+the shock radius 0.3475; binned velocity peak 1.91 against 1.945 for the analytic
+profile binned alike (2.085 right behind the shock); radial momentum 0.328 against
+0.312; kinetic share 0.239 against 0.283."""
 
 import numpy as np
 import pytest
@@ -17,6 +22,7 @@ pytestmark = pytest.mark.gpu
 def test_sedov_blast_radius_and_energy(precision):
     import shamrock_gb300 as sg
     from shamrock_gb300 import setups
+    from shamrock_gb300.sedov import SedovTaylor
 
     s = setups.sedov_taylor(20, jitter=0.0)
     ctx = sg.Context()
@@ -50,8 +56,32 @@ def test_sedov_blast_radius_and_energy(precision):
     mean = np.bincount(idx[ok], weights=rho[ok], minlength=len(edges) - 1) / np.maximum(
         np.bincount(idx[ok], minlength=len(edges) - 1), 1)
     r_peak = 0.5 * (edges[np.argmax(mean)] + edges[np.argmax(mean) + 1])
-    r_th = 1.1517 * (1.0 * t_end**2 / 1.0) ** 0.2
+    sol = SedovTaylor(gamma=s["gamma"], t=t_end, e_blast=1.0, rho0=1.0)
+    r_th = sol.shock_radius
     assert abs(r_peak - r_th) / r_th < 0.1, (r_peak, r_th, steps)
+    # velocity: peak of the binned radial velocity against the post-shock value
+    rhat = (d["xyz"] - 0.5) / np.maximum(r, 1e-300)[:, None]
+    vr = np.sum(d["vxyz"] * rhat, axis=1)
+    vmean = np.bincount(idx[ok], weights=vr[ok], minlength=len(edges) - 1) / np.maximum(
+        np.bincount(idx[ok], minlength=len(edges) - 1), 1)
+    rv_peak = 0.5 * (edges[np.argmax(vmean)] + edges[np.argmax(vmean) + 1])
+    assert abs(rv_peak - r_th) / r_th < 0.1, (rv_peak, r_th)
+    # the analytic v_r at the same particles, binned the same way (the bin holding the
+    # shock averages the post-shock peak with the still gas ahead of it)
+    v_th = sol.profile(r)[1]
+    vmean_th = np.bincount(idx[ok], weights=v_th[ok], minlength=len(edges) - 1) / np.maximum(
+        np.bincount(idx[ok], minlength=len(edges) - 1), 1)
+    assert abs(vmean.max() - vmean_th.max()) / vmean_th.max() < 0.1, (vmean.max(), vmean_th.max())
+    # integrals of the analytic profile
+    rg = np.linspace(0.0, r_th * (1 - 1e-12), 20001)
+    rho_a, v_a, _ = sol.profile(rg)
+    shell = 4 * np.pi * rg * rg
+    p_rad = float(np.sum(s["pmass"] * vr))
+    p_rad_th = float(np.trapezoid(rho_a * v_a * shell, rg))
+    assert abs(p_rad - p_rad_th) / p_rad_th < 0.1, (p_rad, p_rad_th)
+    ekin = float(np.sum(0.5 * s["pmass"] * np.sum(d["vxyz"] ** 2, axis=1)))
+    ekin_th = float(np.trapezoid(0.5 * rho_a * v_a * v_a * shell, rg))  # of E = 1
+    assert abs(ekin / tot["energy"] - ekin_th) / ekin_th < 0.25, (ekin / tot["energy"], ekin_th)
     # a compressed shell: 4 rho0 behind an ideal strong shock, about 1.8 rho0 once SPH
     # smooths it over ~2 h at this resolution (32,000 particles)
     assert mean.max() > 1.5
