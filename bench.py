@@ -52,6 +52,9 @@ def parse():
                         "SPH benchmark, 33,848,064-particle HCP box, varying CD10 viscosity, "
                         "dt = 0 steps")
     p.add_argument("--cells", type=int, default=64, help="FCC cells per axis (4*cells^3 particles)")
+    p.add_argument("--n-target", type=int, default=1 << 25,
+                   help="homogeneous: particle count the HCP box is sized for (the reference's "
+                        "benchmark uses 2^25)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
@@ -61,13 +64,13 @@ def parse():
     return p.parse_args()
 
 
-def workload(cells, kind="sedov"):
+def workload(cells, kind="sedov", n_target=1 << 25):
     """Seeded synthetic inputs with the shapes of the benchmark configurations (no
     dataset is involved).  Returns (set-up dict, name, alpha_AV)."""
     from shamrock_gb300 import setups
 
     if kind == "homogeneous":
-        s = homogeneous_setup(1 << 25)
+        s = homogeneous_setup(n_target)
         name = ("homogeneous_hcp_box_%d (the reference's examples/benchmarks/"
                 "sph_homogeneous_benchmark.py: HCP lattice in the periodic box it closes, rho 1, "
                 "u = 0 but a central injection u_inj W(r, 16 dr), gamma 5/3, M4, varying CD10 "
@@ -371,7 +374,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if not reference_rank_runs(world, rank):
         return 0
-    s, name, alpha_av = workload(args.cells, args.workload)
+    s, name, alpha_av = workload(args.cells, args.workload, args.n_target)
     from oracle import oracle as O
 
     O.set_threads(os.cpu_count())
@@ -445,7 +448,7 @@ def run_gb300(args):
 
     world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
-    s, name, alpha_av = workload(args.cells, args.workload)
+    s, name, alpha_av = workload(args.cells, args.workload, args.n_target)
     n = len(s["h"])
     m = make_model(s, args.precision, device=local, alpha_AV=alpha_av)
     lib = m._lib()
@@ -526,7 +529,7 @@ def run_gb300(args):
         "step_log": {k: log[k] for k in ("h_subcycles", "h_iterations", "corrector_iters",
                                           "next_dt", "cfl_mult")},
     }
-    if args.workload == "homogeneous":
+    if args.workload == "homogeneous" and args.n_target == 1 << 25:
         # the reference's own published figure for this set-up (FP64, varying CD10 AV,
         # 33,848,064 particles, one H100): examples/benchmarks/sph_homogeneous_bench_result.json
         line["published_reference"] = {

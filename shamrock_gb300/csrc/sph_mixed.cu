@@ -147,12 +147,14 @@ __global__ void k_stage_hydro(u32 N, const f64 *__restrict__ x, const f64 *__res
 // derivatives kernel.  c_s is stored in FP32, so it and the LP07 power are
 // evaluated in FP32 (relative error ~2e-7, the size of the records' own rounding); rho,
 // P and 1/(rho^2 Omega) stay FP64 until they are split into the record.
-// varying viscosity: the accelerations of the last evaluation as FP32 records (ghosts
-// copy their source) and the plain sound speed per rank (the records' c_s lane then
-// carries alpha c_s)
+// varying viscosity: per rank a 32-byte record V of what the velocity gradients read
+// besides positions, {vx_hi, vy_hi, vz_hi, ax | ay, az, bf16 (vx_lo, vy_lo), bf16 (vz_lo, 0)},
+// the accelerations being those of the last evaluation in FP32 (ghosts copy their
+// source), and the plain sound speed per rank (the records' c_s lane then carries
+// alpha c_s)
 struct StageAV {
     const f64 *ax, *ay, *az; // caller's local fields, stride of the caller's vectors
-    float4 *A;               // null: constant viscosity
+    float4 *V;               // 2 float4 per rank; null: constant viscosity
     float *cs_rank;
 };
 
@@ -209,9 +211,10 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
     P[p2 + 1] = make_float4(xl, yl, zl, cs);
     H[p2]     = make_float4(vxh, vyh, vzh, __double2float_rn(uu));
     H[p2 + 1] = make_float4(Ph, c1, pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, Pl));
-    if (av.A) {
-        av.A[r]       = make_float4(__double2float_rn(av.ax[iv]), __double2float_rn(av.ay[iv]),
-                                    __double2float_rn(av.az[iv]), 0.f);
+    if (av.V) {
+        av.V[p2]     = make_float4(vxh, vyh, vzh, __double2float_rn(av.ax[iv]));
+        av.V[p2 + 1] = make_float4(__double2float_rn(av.ay[iv]), __double2float_rn(av.az[iv]),
+                                   pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, 0.f));
         av.cs_rank[r] = cs;
     }
 }
@@ -485,8 +488,14 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
 // ---- varying viscosity, FP32 pair arithmetic: div v, curl v (SPH estimates) and
 // d(div v)/dt = tr(G(a)) - tr(G(v) G(v)) with the corrected gradients G = R^-1 D, the
 // mass factoring out of R^-1 D.  Positions and velocities from the hi/lo records,
-// accelerations from the FP32 acceleration records; FP32 sums (the results feed the
-// viscosity switch, not the state).  Same pairs, kernel and order of terms as k_velgrad64.
+// accelerations from the V records (64 bytes per pair with the position records); FP32
+// sums (the results feed the viscosity switch, not the state).  The same sums as
+// k_velgrad64, arranged for FP32:
+//  - only pairs inside a's kernel support are visited (the cache also holds pairs inside
+//    b's only, whose dW(r, h_a) is zero);
+//  - R = -sum r (x) g is symmetric (g is parallel to r): six sums;
+//  - div v and curl v are read off Dv = -sum g (x) v: sum v.g = -tr Dv and
+//    sum (v x g)_i = eps_ijk Dv[k][j] (the SPH sums are the same terms as Dv's).
 __device__ __forceinline__ void inv33f(const float m[3][3], float r[3][3]) {
     const float a00 = m[0][0], a01 = m[0][1], a02 = m[0][2];
     const float a10 = m[1][0], a11 = m[1][1], a12 = m[1][2];
@@ -506,7 +515,7 @@ __device__ __forceinline__ void inv33f(const float m[3][3], float r[3][3]) {
 }
 
 __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace ms,
-                                                       const float4 *__restrict__ A,
+                                                       const float4 *__restrict__ V,
                                                        const f64 *__restrict__ omega_local,
                                                        f64 pmass, float mh3,
                                                        f64 *__restrict__ divv, f64 *__restrict__ cx,
@@ -517,25 +526,23 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
     const u32 a  = rs.row_rank[t];
     const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
     const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
-    const F8 ha = ldg256(&ms.H[2 * (size_t) a]);
-    const float4 aa = __ldg(&A[a]);
+    const F8 va = ldg256(&V[2 * (size_t) a]);
     const float hia = pa.a.w, hia2 = hia * hia;
     const float k4a = hia2 * hia2 * kNorm3dF;
-    const float vla[3] = {bf_hi(ha.b.z), bf_lo(ha.b.z), bf_hi(ha.b.w)};
-    float sdiv = 0.f, sc[3] = {0.f, 0.f, 0.f};
-    float R[3][3] = {}, Dv[3][3] = {}, Da[3][3] = {};
+    const float vla[3] = {bf_hi(va.b.z), bf_lo(va.b.z), bf_hi(va.b.w)};
+    const float aa[3]  = {va.a.w, va.b.x, va.b.y};
+    float R00 = 0.f, R01 = 0.f, R02 = 0.f, R11 = 0.f, R12 = 0.f, R22 = 0.f;
+    float Dv[3][3] = {}, Da[3][3] = {};
     // entries four at a time (pipeline rows are padded to 4), all records of the four
     // neighbours requested together, the next four entries fetched behind them
     uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, true, a) : make_uint4(a, a, a, a);
     for (u32 k = k0; k < k1; k += 4) {
         const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
-        F8 pb[4], hb[4];
-        float4 ab[4];
+        F8 pb[4], vb[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             pb[q] = ldg256(&ms.P[2 * (size_t) bb[q]]);
-            hb[q] = ldg256(&ms.H[2 * (size_t) bb[q]]);
-            ab[q] = __ldg(&A[bb[q]]);
+            vb[q] = ldg256(&V[2 * (size_t) bb[q]]);
         }
         if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, true, a);
 #pragma unroll
@@ -544,25 +551,25 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
                                 (pa.a.y - pb[q].a.y) + (pa.b.y - pb[q].b.y),
                                 (pa.a.z - pb[q].a.z) + (pa.b.z - pb[q].b.z)};
             const float r2  = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
-            const float hib = pb[q].a.w;
-            if (k + q >= k1 || (r2 * hia2 > 4.f && r2 * (hib * hib) > 4.f)) continue;
+            if (k + q >= k1 || r2 * hia2 > 4.f) continue;
             const float rab  = sqrtf(r2);
-            const float v[3] = {(ha.a.x - hb[q].a.x) + (vla[0] - bf_hi(hb[q].b.z)),
-                                (ha.a.y - hb[q].a.y) + (vla[1] - bf_lo(hb[q].b.z)),
-                                (ha.a.z - hb[q].a.z) + (vla[2] - bf_hi(hb[q].b.w))};
-            const float w[3] = {aa.x - ab[q].x, aa.y - ab[q].y, aa.z - ab[q].z};
+            const float v[3] = {(va.a.x - vb[q].a.x) + (vla[0] - bf_hi(vb[q].b.z)),
+                                (va.a.y - vb[q].a.y) + (vla[1] - bf_lo(vb[q].b.z)),
+                                (va.a.z - vb[q].a.z) + (vla[2] - bf_hi(vb[q].b.w))};
+            const float w[3] = {aa[0] - vb[q].a.w, aa[1] - vb[q].b.x, aa[2] - vb[q].b.y};
             const float inv  = (rab < 1e-9f) ? 0.f : __frcp_rn(rab);
             const float F    = k4a * m4_df32(rab * hia) * inv; // dW(r, h_a) / r
             const float g[3] = {F * r[0], F * r[1], F * r[2]};
-            sdiv  = sdiv + ((v[0] * g[0] + v[1] * g[1]) + v[2] * g[2]);
-            sc[0] = sc[0] + (v[1] * g[2] - v[2] * g[1]);
-            sc[1] = sc[1] + (v[2] * g[0] - v[0] * g[2]);
-            sc[2] = sc[2] + (v[0] * g[1] - v[1] * g[0]);
+            R00 = R00 - r[0] * g[0];
+            R01 = R01 - r[0] * g[1];
+            R02 = R02 - r[0] * g[2];
+            R11 = R11 - r[1] * g[1];
+            R12 = R12 - r[1] * g[2];
+            R22 = R22 - r[2] * g[2];
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
-                    R[i][j]  = R[i][j] - r[i] * g[j];
                     Dv[j][i] = Dv[j][i] - v[i] * g[j];
                     Da[j][i] = Da[j][i] - w[i] * g[j];
                 }
@@ -571,10 +578,11 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
     const u32 i = rs.row_local[t];
     const float rho_a = mh3 * hia2 * hia;
     const float f = -(float) pmass / (__double2float_rn(omega_local[i]) * rho_a);
-    divv[i] = (f64) (f * sdiv);
-    cx[(size_t) i * cvs] = (f64) (f * sc[0]);
-    cy[(size_t) i * cvs] = (f64) (f * sc[1]);
-    cz[(size_t) i * cvs] = (f64) (f * sc[2]);
+    divv[i] = (f64) (-f * ((Dv[0][0] + Dv[1][1]) + Dv[2][2]));
+    cx[(size_t) i * cvs] = (f64) (f * (Dv[1][2] - Dv[2][1]));
+    cy[(size_t) i * cvs] = (f64) (f * (Dv[2][0] - Dv[0][2]));
+    cz[(size_t) i * cvs] = (f64) (f * (Dv[0][1] - Dv[1][0]));
+    const float R[3][3] = {{R00, R01, R02}, {R01, R11, R12}, {R02, R12, R22}};
     float Ri[3][3], G[3][3];
     inv33f(R, Ri);
     float div_a = 0.f;
@@ -665,9 +673,9 @@ cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf
     StageAV av{lf.ax, lf.ay, lf.az, nullptr, nullptr};
     if (varying_av) {
         cudaError_t e;
-        if ((e = c.f_aux1.ensure(sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
+        if ((e = c.f_aux1.ensure(2 * sizeof(float4) * (size_t) N, c.stream)) != cudaSuccess) return e;
         if ((e = c.f_aux2.ensure(sizeof(float) * (size_t) N, c.stream)) != cudaSuccess) return e;
-        av.A       = c.f_aux1.as<float4>();
+        av.V       = c.f_aux1.as<float4>();
         av.cs_rank = c.f_aux2.as<float>();
     }
     StageEos se{eos.kind, eos.gamma - 1, pmass * kHfact * kHfact * kHfact,
