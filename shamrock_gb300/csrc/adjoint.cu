@@ -48,6 +48,19 @@ __device__ __forceinline__ T m4_d2(T q) {
     if (q < T(1)) return T(-3) + T(4.5) * q;
     return q < T(2) ? T(3) - T(1.5) * q : T(0);
 }
+// Division and square root of the pair loops: exact in FP64 (the reference gradient),
+// the hardware approximations in FP32 (about 2 ulp: the FP32 reverse pass is checked
+// against central differences at the 1e-6 level, and the correctly rounded forms cost
+// many more instructions per pair)
+template<class T>
+__device__ __forceinline__ T pdiv(T a, T b) { return a / b; }
+template<>
+__device__ __forceinline__ float pdiv<float>(float a, float b) { return __fdividef(a, b); }
+template<class T>
+__device__ __forceinline__ T psqrt(T x) { return sqrt(x); }
+template<>
+__device__ __forceinline__ float psqrt<float>(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+
 template<class T>
 __device__ __forceinline__ T rho_of_h(T m, T h) {
     const T r = T(kHfact) / h;
@@ -275,16 +288,17 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             const T hb = nb.h;
             if (r2 > hc * hc * Rk2 && r2 > hb * hb * Rk2) continue;
             if (r2 == T(0)) continue; // self pair: no contribution and no dependence
-            const T r = sqrt(r2), ir = T(1) / r;
+            const T r = psqrt(r2), ir = pdiv(T(1), r);
             const T ex = dx * ir, ey = dy * ir, ez = dz * ir;
             const T ub = nb.u, omb = nb.om;
             const T rhob = rho_of_h(m, hb);
             const T csqb = lp07 ? cs0sq * pow(nb.rsq * ir0sq, mq) : gam * gm1 * ub;
             const T Pb   = lp07 ? csqb * rhob : gm1 * rhob * ub;
-            const T csb  = sqrt(csqb);
+            const T csb  = psqrt(csqb);
             const T subb = rhob * rhob * omb;
-            const T kb = (subb != T(0) && subb == subb) ? T(1) / subb : T(0), jb = T(1) / (rhob * omb);
-            const T ihb = T(1) / hb;
+            const T kb = (subb != T(0) && subb == subb) ? pdiv(T(1), subb) : T(0),
+                    jb = pdiv(T(1), rhob * omb);
+            const T ihb = pdiv(T(1), hb);
             const T qc = r * ihc, qb = r * ihb;
             const T ihb4 = ihb * ihb * ihb * ihb;
             const T d1c = m4_d1(qc), d1b = m4_d1(qb), d2c = m4_d2(qc), d2b = m4_d2(qb);
@@ -302,7 +316,7 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             const T wb = actb ? T(1) : (tb == T(0) ? half : T(0));
             const T Ac = Pc + (actc ? tc : T(0)), Ab = Pb + (actb ? tb : T(0));
             const T dP = Pc - Pb, rbar = half * (rhoc + rhob);
-            const T vsu = sqrt(fabs(dP) / rbar);
+            const T vsu = psqrt(pdiv(fabs(dP), rbar));
             const T J = Fc * jc + Fb * jb;
             const T S = Ac * kc * Fc + Ab * kb * Fb;
             const T Lx = lxc - nb.lx, Ly = lyc - nb.ly, Lz = lzc - nb.lz;
@@ -332,11 +346,11 @@ __global__ void __launch_bounds__(128) k_adj_derivs(RowSpace rs, Src src, AdjPar
             // particle-c scalars
             const T dLAc  = -m * Le * kc * Fc + m * w * muc * kc * Fc;
             const T dLvsu = half * m * au * dmu * du_ * J;
-            const T dvsuP = vsu > T(0) ? (dP > T(0) ? T(1) : T(-1)) / (T(2) * rbar * vsu) : T(0);
-            const T dvsur = vsu > T(0) ? -vsu / (T(4) * rbar) : T(0);
+            const T dvsuP = vsu > T(0) ? pdiv(dP > T(0) ? T(1) : T(-1), T(2) * rbar * vsu) : T(0);
+            const T dvsur = vsu > T(0) ? pdiv(-vsu, T(4) * rbar) : T(0);
             sP += dLAc + dLvsu * dvsuP;
             if (actc) scs += dLAc * (-half * rhoc * aAV * w);
-            srho += (actc ? dLAc * (tc / rhoc) : T(0)) + dLvsu * dvsur;
+            srho += (actc ? dLAc * pdiv(tc, rhoc) : T(0)) + dLvsu * dvsur;
             sk += -m * Le * Ac * Fc + m * w * muc * Ac * Fc;
             sj += cond * Fc;
             su += half * m * au * dmu * vsu * J;
@@ -409,7 +423,7 @@ __global__ void __launch_bounds__(256) k_adj_omega_a(RowSpace rs, Src src, const
         T dx, dy, dz, hb;
         if constexpr (std::is_same<T, f64>::value) src.dpos(b, px, py, pz, dx, dy, dz, hb);
         else src.dpos(b, pc, dx, dy, dz, hb);
-        const T q = sqrt(dx * dx + dy * dy + dz * dz) * ihc;
+        const T q = psqrt(dx * dx + dy * dy + dz * dz) * ihc;
         if (q >= T(2)) continue;
         const T f0 = m4_f(q), f1 = m4_d1(q), f2 = m4_d2(q);
         S += -sig * (T(3) * f0 + q * f1) * ih4;
@@ -450,8 +464,8 @@ __global__ void __launch_bounds__(256) k_adj_omega_b(RowSpace rs, Src src, f64 p
         else src.dpos(b, pc, dx, dy, dz, hb);
         const T r2 = dx * dx + dy * dy + dz * dz;
         if (r2 == T(0)) continue;
-        const T r = sqrt(r2), ir = T(1) / r;
-        const T ihb = T(1) / hb;
+        const T r = psqrt(r2), ir = pdiv(T(1), r);
+        const T ihb = pdiv(T(1), hb);
         const T qc = r * ihc, qb = r * ihb;
         if (qc >= T(2) && qb >= T(2)) continue;
         T nub, lomb;

@@ -387,12 +387,12 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
             float rinv = rsqrtf(r2);
             float rab  = r2 * rinv;
             float Fa   = k4a * m4_df32(rab * hia);
-            float Fb   = hib3 * hib * kNorm3dF * m4_df32(rab * hib);
-            float rx = dx * rinv, ry = dy * rinv, rz = dz * rinv;
+            float Fb   = (hib2 * hib2) * kNorm3dF * m4_df32(rab * hib);
             float vx = (ha.a.x - hb[j].a.x) + (vla_x - bf_hi(hb[j].b.z));
             float vy = (ha.a.y - hb[j].a.y) + (vla_y - bf_lo(hb[j].b.z));
             float vz = (ha.a.z - hb[j].a.z) + (vla_z - bf_hi(hb[j].b.w));
-            float vr  = vx * rx + vy * ry + vz * rz;
+            // r_hat = (dx, dy, dz) rinv applied once to v.r and once to the force
+            float vr  = (vx * dx + vy * dy + vz * dz) * rinv;
             float avr = fabsf(vr);
             float vsig_a = p.alpha_AV * cs_a + p.beta_AV * avr;
             float vsig_b = p.alpha_AV * cs_b + p.beta_AV * avr;
@@ -402,10 +402,10 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
             float qa = fmaxf(-0.5f * rho_a * vsig_a * vr, 0.f);
             float qb = fmaxf(-0.5f * rho_b * vsig_b * vr, 0.f);
             float AVPa = P_a + qa, AVPb = P_b + qb;
-            float f    = AVPa * c1a * Fa + AVPb * c1b * Fb;
-            bx += f * rx;
-            by += f * ry;
-            bz += f * rz;
+            float f    = (AVPa * c1a * Fa + AVPb * c1b * Fb) * rinv;
+            bx += f * dx;
+            by += f * dy;
+            bz += f * dz;
             bu += AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - hb[j].a.w) * (Fa * c2a + Fb * c2b);
             vsig_max = fmaxf(vsig_max, cs_sig + 2.f * avr);
         }
@@ -557,12 +557,12 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
                                 (pa.a.z - pb[q].a.z) + (pa.b.z - pb[q].b.z)};
             const float r2  = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
             if (k + q >= k1 || r2 * hia2 > 4.f) continue;
-            const float rab  = sqrtf(r2);
+            const float inv  = (r2 < 1e-18f) ? 0.f : rsqrtf(r2); // 1/r, 0 for coincident pairs
+            const float rab  = r2 * inv;
             const float v[3] = {(va.a.x - vb[q].a.x) + (vla[0] - bf_hi(vb[q].b.z)),
                                 (va.a.y - vb[q].a.y) + (vla[1] - bf_lo(vb[q].b.z)),
                                 (va.a.z - vb[q].a.z) + (vla[2] - bf_hi(vb[q].b.w))};
             const float w[3] = {aa[0] - vb[q].a.w, aa[1] - vb[q].b.x, aa[2] - vb[q].b.y};
-            const float inv  = (rab < 1e-9f) ? 0.f : __frcp_rn(rab);
             const float F    = k4a * m4_df32(rab * hia) * inv; // dW(r, h_a) / r
             const float g[3] = {F * r[0], F * r[1], F * r[2]};
             R00 = R00 - r[0] * g[0];
