@@ -236,12 +236,6 @@ class PhantomDump:
         self.tables = {kind: PhantomDumpTableHeader(kind) for kind, _ in TYPE_KINDS}
         self.blocks: list[PhantomDumpBlock] = []
 
-    # -- the typed tables under the reference's member names
-    def __getattr__(self, name):
-        if name.startswith("table_header_") and name[13:] in _KIND_DTYPE:
-            return self.__dict__["tables"][name[13:]]
-        raise AttributeError(name)
-
     def override_magic_number(self):
         self.i1, self.i2, self.i3 = MAGIC_I1, MAGIC_I2, MAGIC_I3
         self.r1 = float(self.i2)
@@ -335,6 +329,13 @@ class PhantomDump:
             print("block ", i, ":", file=out)
             b.print_state(out)
         print("------------------", file=out)
+
+
+# the typed tables under the reference's member names (table_header_fort_int, ...)
+for _kind, _ in TYPE_KINDS:
+    setattr(PhantomDump, "table_header_" + _kind,
+            property(lambda self, k=_kind: self.tables[k], doc=f"the {_kind} header table"))
+del _kind
 
 
 def load_phantom_dump(fname: str) -> PhantomDump:
