@@ -65,7 +65,8 @@ class _Writer:
     def __init__(self):
         self.parts = []
 
-    def record(self, payload: bytes):
+    def record(self, payload):
+        """payload: bytes or a byte view (arrays are kept as views until written)."""
         n = len(payload)
         if n > _MAX_RECORD:
             raise FortranIOError(f"a Fortran record of {n} bytes exceeds the 4-byte record length")
@@ -85,7 +86,7 @@ class _Writer:
         a = np.ascontiguousarray(vals, dtype=dtype)
         if count > a.size:
             raise FortranIOError("val count is higher than vec size")
-        self.record(a[:count].tobytes())
+        self.record(memoryview(np.ascontiguousarray(a[:count])).cast("B"))
 
     def getvalue(self) -> bytes:
         return b"".join(self.parts)
@@ -248,6 +249,9 @@ class PhantomDump:
     # -- file I/O
     def gen_file(self) -> bytes:
         """The dump as the bytes of a Phantom file (PhantomDump::gen_file)."""
+        return self._records().getvalue()
+
+    def _records(self) -> _Writer:
         w = _Writer()
         w.values("idiii", self.i1, self.r1, self.i2, self.iversion, self.i3)
         w.string(self.fileid, 100)
@@ -261,11 +265,13 @@ class PhantomDump:
                 for a in b.arrays[kind]:
                     w.string(a.tag, 16)
                     w.array(a.vals, dt, b.tot_count)
-        return w.getvalue()
+        return w
 
     def save_dump(self, fname: str):
+        """Writes the records one by one (no whole-file copy in memory)."""
+        parts = self._records().parts
         with open(fname, "wb") as f:
-            f.write(self.gen_file())
+            f.writelines(parts)
 
     @classmethod
     def from_bytes(cls, data: bytes) -> "PhantomDump":
