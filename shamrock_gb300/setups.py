@@ -124,7 +124,9 @@ def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0, jitter=0.1):
 def sound_wave(n_side=64, amp=1e-4, gamma=1.0001, cs=1.0, travelling=True, noise=1e-4,
                seed=12345):
     """n_side^3 particles on a simple cubic lattice (sites at (i + 1/2) / n_side), then
-    rho = 1 + amp sin(2 pi x) by the first-order remap x -> x - amp/(2 pi) cos(2 pi x);
+    rho = 1 + amp sin(2 pi x) by the first-order remap x -> x + amp/(2 pi) cos(2 pi x)
+    (the displacement's derivative is -amp sin(2 pi x), so the spacing shrinks where
+    sin > 0);
     P = cs^2 / gamma at rho = 1 (u = P / ((gamma - 1) rho)).  travelling: the acoustic
     wave's own velocity v_x = amp cs sin(2 pi x) (a wave moving in +x); else at rest.
     noise: seeded perturbations, velocity N(0, (noise cs)^2) per component and u relative
@@ -137,7 +139,7 @@ def sound_wave(n_side=64, amp=1e-4, gamma=1.0001, cs=1.0, travelling=True, noise
     pos = np.stack([i.ravel(), j.ravel(), k.ravel()], 1)
     N = pos.shape[0]
     x = pos[:, 0]
-    pos[:, 0] = np.mod(x - amp / (2 * np.pi) * np.cos(2 * np.pi * x), 1.0)
+    pos[:, 0] = np.mod(x + amp / (2 * np.pi) * np.cos(2 * np.pi * x), 1.0)
     pmass = 1.0 / N
     rho = 1.0 + amp * np.sin(2 * np.pi * pos[:, 0])
     P0 = cs * cs / gamma
