@@ -252,3 +252,23 @@ def test_units_and_eos_conversions():
         assert P.eos_config_from_dump(d3, bypass_error=True) is None
     with pytest.raises(ValueError):
         P._read_headeropts_eos(d3, 2)
+
+
+def test_sink_block_is_refused():
+    """Sink particles are not on the GB300 path: a dump holding any raises on loading
+    (an empty sink block, as Phantom writes without sinks, is accepted)."""
+    m, _ = _model("constant", "adiabatic", True)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        dump = m.make_phantom_dump()
+    empty = P.PhantomDumpBlock(0)
+    dump.blocks.append(empty)
+    m2 = sg.get_Model_SPH(context=sg.Context(), vector_type="f64_3", sph_kernel="M4")
+    m2.init_from_phantom_dump(dump)
+    assert m2.get_total_part_count() == m.get_total_part_count()
+    sinks = P.PhantomDumpBlock(1)
+    for k in ("x", "y", "z", "m", "h", "vx", "vy", "vz"):
+        sinks.set_array("fort_real", k, [0.5])
+    dump.blocks[1] = sinks
+    with pytest.raises(NotImplementedError):
+        m2.init_from_phantom_dump(dump)
