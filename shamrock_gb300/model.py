@@ -591,6 +591,8 @@ class Model:
         self.set_time(dump.read_header_float("time"))
         pos = np.stack([x, y, z], 1)
         keep = np.all((pos >= self.box_min) & (pos < self.box_max), axis=1) & (h >= 0)
+        if keep.all():
+            keep = slice(None)  # views: set_particles makes the one copy
         if v.size == 0:
             v = np.zeros((x.size, 3))
         self.set_particles(pos[keep], v[keep], h[keep] * hpart_fact_load,
