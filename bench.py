@@ -25,6 +25,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -41,7 +42,11 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--precision", default="mixed",
+                   choices=["mixed", "mixed_fp32", "mixed_compensated", "fp64"],
+                   help="mixed: error-controlled (FP32 pair arithmetic, compensated where the "
+                        "step's error estimate exceeds 1e-5); mixed_fp32: FP32 without the "
+                        "control; mixed_compensated: the compensated tier on every step")
     p.add_argument("--workload", default="sedov",
                    choices=["sedov", "sedov_plain", "clustered", "soundwave", "disc", "homogeneous"],
                    help="sedov: jittered Sedov-Taylor (default, 4*cells^3); sedov_plain: the "
@@ -163,7 +168,9 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+        # a private temporary file (BENCH_CLOCKS_CSV keeps the samples somewhere chosen)
+        self.path = os.environ.get("BENCH_CLOCKS_CSV") or os.path.join(
+            tempfile.gettempdir(), f"gbsph_bench_clocks_{os.getpid()}_rank{device}.csv")
 
     def __enter__(self):
         try:
@@ -215,18 +222,19 @@ class ClockSampler:
 # L1/L2 hits; index streams and per-particle fields are counted).  units: rows (local
 # particles), entries (CSR entries), keys (sorted slots).
 def stage_bytes(stage, n, N, entries, P, precision, h_iters):
-    vec = 64 if precision == "mixed" else 88
+    mixed = precision.startswith("mixed")
+    vec = 64 if mixed else 88
     table = {
         # row_rank, row_local, cnt, off, own fields, CSR entries, caller a/du/v/u in+out,
         # h; every particle's record read once from DRAM (further gathers: L1/L2 hits)
         "derivs": n * (16 + vec + 128 + 8) + 4 * entries + N * vec,
         # per Newton iteration: CSR entries + own position + per-row h/eps state
-        "h_iterate": (n * (16 + (32 if precision == "mixed" else 24) + 40) + 4 * entries) * h_iters,
+        "h_iterate": (n * (16 + (32 if mixed else 24) + 40) + 4 * entries) * h_iters,
         "cache_fill": n * (4 + 4 + 4 + 32) + 4 * entries,
         "cache_count": n * (4 + 4 + 4 + 32),
         "omega": n * (16 + 32 + 8 + 8) + 4 * entries,
         "morton_sort": 16 * P,
-        "gather_eos": N * (4 + 4 + 8 * 8) + N * (80 if precision == "mixed" else 64),
+        "gather_eos": N * (4 + 4 + 8 * 8) + N * (80 if mixed else 64),
     }
     return table.get(stage)
 
@@ -336,6 +344,26 @@ def oracle_config(O, s, alpha_AV):
     return oc
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
+
+
 def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     """FP64 oracle (OpenMP) on the same workload, bounded to about `seconds`."""
     from oracle import oracle as O
@@ -357,6 +385,7 @@ def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
             break
     el = time.time() - t0
     return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": f"{steps} FP64 oracle steps of {what} ({n} particles) after one "
                       f"untimed dt=0 step, {el:.1f} s, OpenMP {cores} threads"}
 
@@ -383,7 +412,9 @@ def run_reference(args):
     oc = oracle_config(O, s, alpha_av)
     sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
     n = len(s["h"])
-    for _ in range(max(1, min(args.warmup, 2))):
+    # the requested untimed warm-up steps (at least one: the first step converges h)
+    warm = max(1, args.warmup)
+    for _ in range(warm):
         ostep(sim, s)
     budget = 150.0
     t0 = time.time()
@@ -397,33 +428,50 @@ def run_reference(args):
     value = n * steps / el
     sample = (f"{steps} of {args.steps} requested FP64 steps of {what} ({n} particles; "
               f"stopped at a {budget:.0f} s budget if reached), after "
-              f"{max(1, min(args.warmup, 2))} untimed warm-up steps")
+              f"{warm} untimed warm-up steps")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3,
+            "steps": steps, "warmup": warm, "ms_per_step": el / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": name, "precision": "fp64", "particles": n,
                        "implementation": "FP64 CPU restatement of the reference path (oracle/, "
                                          "OpenMP); the reference itself needs a SYCL compiler"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "cpu_model": cpu_model(), "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def accuracy(s, alpha_AV=1.0):
+def precision_control(logs):
+    """Which tier the timed steps ran in and the FP32 tier's estimated errors."""
+    n = max(len(logs), 1)
+    return {"steps_fp32": sum(1 for g in logs if g["tier"] == 1),
+            "steps_compensated": sum(1 for g in logs if g["tier"] == 2),
+            "steps_fp64": sum(1 for g in logs if g["tier"] == 0),
+            "reruns": sum(int(g["tier_reruns"]) for g in logs),
+            "compensated_fraction": sum(1 for g in logs if g["tier"] == 2) / n,
+            "fp32_err_est_max": {"a": max(g["err_est_a"] for g in logs) if logs else None,
+                                 "du_dt": max(g["err_est_du"] for g in logs) if logs else None},
+            "definition": "tier per timed step (error-controlled mixed precision: FP32 pair "
+                          "arithmetic while the estimated error of the FP32 tier stays within "
+                          "1e-5, else the compensated tier; a rerun recomputes a step that "
+                          "started in FP32 compensated); estimates relative to each field's "
+                          "largest magnitude"}
+
+
+def accuracy(s, alpha_AV=1.0, precision="mixed"):
     """Max / RMS relative error of rho, |a|, du/dt and v_sig-driven dt of one mixed step
     against one FP64 step from the same initial state (the first, dt = 0, step)."""
     import numpy as np
 
     res = {}
     d = {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", precision):
         m = make_model(s, prec, alpha_AV=alpha_AV)
         m.evolve_once()
         d[prec] = m.collect_data()
-    a, b = d["mixed"], d["fp64"]
+    a, b = d[precision], d["fp64"]
     rho_a = s["pmass"] * (1.2 / a["hpart"]) ** 3
     rho_b = s["pmass"] * (1.2 / b["hpart"]) ** 3
     rel = np.abs(rho_a - rho_b) / rho_b
@@ -515,7 +563,7 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32-mixed" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "dtype": "fp32-mixed" if args.precision.startswith("mixed") else "f64", "data": "synthetic",
         "config": {"workload": name, "precision": args.precision, "particles": n,
                    "ghosts": int(log["n_ghost"]), "leaves": int(log["leaf_count"]),
                    "cache_entries": int(log["cache_size"]),
@@ -528,6 +576,7 @@ def run_gb300(args):
         "roofline": rl,
         "step_log": {k: log[k] for k in ("h_subcycles", "h_iterations", "corrector_iters",
                                           "next_dt", "cfl_mult")},
+        "precision_control": precision_control(logs),
     }
     if args.workload == "homogeneous" and args.n_target == 1 << 25:
         # the reference's own published figure for this set-up (FP64, varying CD10 AV,
@@ -536,7 +585,7 @@ def run_gb300(args):
             "value": 25502056.0, "unit": UNIT, "hardware": "NVIDIA H100, DPC++, 1 rank",
             "precision": "fp64", "this_over_published": value / 25502056.0}
     if world == 1 and not args.no_accuracy:
-        line["accuracy_mixed_vs_fp64"] = accuracy(s, alpha_AV=alpha_av)
+        line["accuracy_mixed_vs_fp64"] = accuracy(s, alpha_AV=alpha_av, precision=args.precision)
         # FP64 GPU rate on the same workload (the x3 denominator), a few steps
         m64 = make_model(s, "fp64", alpha_AV=alpha_av)
         for _ in range(2):
@@ -551,7 +600,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         v64 = n * k64 / (g0.elapsed_time(g1) * 1e-3)
         line["fp64_gpu"] = {"value": v64, "unit": UNIT, "steps": k64}
-        if args.precision == "mixed":
+        if args.precision.startswith("mixed"):
             line["mixed_over_fp64"] = value / v64
     if world == 1 and not args.no_adjoint:
         if args.workload == "disc":

@@ -41,6 +41,19 @@ extern "C" {
 
 #define GBSPH_FP64 0  /* every pair sum in FP64, bit-identical to the FP64 oracle */
 #define GBSPH_MIXED 1 /* FP32 pair arithmetic, FP64 positions/drift/h test/totals */
+/* FP32 pair arithmetic with the sums that cancel in double-float (two floats per value,
+ * error-free transformations on the FP32 pipes): h finished by one double-float Newton
+ * step, Omega, and the background-pressure part of the force.  For use where GBSPH_MIXED
+ * loses accuracy to cancellation (a large uniform pressure, e.g. a sound wave: 1e-6 of
+ * the FP64 path where GBSPH_MIXED errs by 4e-3). */
+#define GBSPH_MIXED_COMPENSATED 2
+/* Error-controlled mixed precision (gbsph_evolve_once): each step estimates the error of
+ * the FP32 tier from condition sums the derivatives pass accumulates (the summed pair
+ * force and du/dt magnitudes against the largest result); a step whose estimate exceeds
+ * gbsph_config.mixed_tol is recomputed from its start state in the compensated tier, and
+ * later steps stay there until the estimate falls below a quarter of the tolerance.
+ * gbsph_step_log reports the tier, reruns and estimates. */
+#define GBSPH_MIXED_GUARDED 3
 
 typedef struct gbsph_ctx gbsph_ctx;
 
@@ -83,7 +96,7 @@ typedef struct {
     uint32_t tree_reduction_level;  /* 3 */
     uint32_t periodic;              /* 1 periodic box, 0 free boundaries */
     double box_min[3], box_max[3];
-    uint32_t precision;             /* GBSPH_FP64 or GBSPH_MIXED */
+    uint32_t precision;             /* GBSPH_FP64, GBSPH_MIXED, _COMPENSATED or _GUARDED */
     uint32_t pad;
     /* Per-particle Newton threshold: a particle's h is updated while its eps_h exceeds
      * it (1e-6 in the reference's IterateSmoothingLengthDensity kernel; 0 selects
@@ -112,6 +125,10 @@ typedef struct {
     uint32_t av_kind;
     uint32_t pad2;
     double alpha_min, alpha_max, sigma_decay;
+    /* GBSPH_MIXED_GUARDED: the largest estimated error of a step's accelerations and du/dt
+     * (relative to the largest magnitude of each field) the FP32 tier may leave; 0 selects
+     * 1e-5. */
+    double mixed_tol;
 } gbsph_config;
 
 #define GBSPH_EOS_ADIABATIC 0
@@ -135,6 +152,13 @@ typedef struct {
     double eps_v, max_eps_h;
     double elapsed_s; /* wall time of the step (host clock, after the final sync) */
     double rate;      /* n_local / elapsed_s, as Solver.cpp:3200 */
+    /* mixed precision: the tier that produced the step (GBSPH_FP64, GBSPH_MIXED or
+     * GBSPH_MIXED_COMPENSATED), whether a GBSPH_MIXED_GUARDED step was recomputed in the
+     * compensated tier (1) or not (0), and the estimated error of the FP32 tier's
+     * accelerations and du/dt on the last corrector evaluation (relative to the largest
+     * magnitude of each field; 0 in FP64) */
+    uint32_t tier, tier_reruns;
+    double err_est_a, err_est_du;
 } gbsph_step_log;
 
 /* ------------------------------------------------------------------ lifetime */
@@ -259,8 +283,10 @@ int gbsph_derivs_constAV(gbsph_ctx *ctx, const uint32_t *cnt, const uint32_t *sc
  *  - The FP32 staging lives in a fixed device array inside the library, sized for at
  *    most 65,536 merged particles (4 MiB, reserved on every GPU that loads the library
  *    until the process exits); larger n_merged returns GBSPH_ERR_CAPACITY.
- *  - The first call on a device looks the array's device address up; make that first
- *    call before any stream capture.
+ *  - Every call looks the array's device address up in the current context (a cached
+ *    address would be wrong after cudaDeviceReset or under another context on the same
+ *    device).  The first call in a context also loads the library's device code: make
+ *    that first call before any stream capture.
  *  - All calls share the one array: calls that overlap on the GPU (other streams, other
  *    threads) race; serialise them.  Nothing needs clearing between calls.
  *  - Asynchronous on `stream`; returns GBSPH_OK, GBSPH_ERR_CAPACITY, GBSPH_ERR_ARG or

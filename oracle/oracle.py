@@ -56,8 +56,9 @@ class OrcStepLog(C.Structure):
 
 def build(force=False):
     """Compile the oracle with its Makefile (seconds)."""
+    srcs = [os.path.join(HERE, f) for f in ("gbsph_oracle.cpp", "Makefile")]
     if force or not os.path.exists(LIB_PATH) or (
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "gbsph_oracle.cpp"))):
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs)):
         subprocess.check_call(["make", "-s", "-C", HERE])
 
 

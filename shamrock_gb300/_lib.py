@@ -18,6 +18,8 @@ GBSPH_ERR_NOT_CONVERGED = 4
 GBSPH_ERR_STATE = 5
 GBSPH_FP64 = 0
 GBSPH_MIXED = 1
+GBSPH_MIXED_COMPENSATED = 2
+GBSPH_MIXED_GUARDED = 3
 GBSPH_AV_CONSTANT = 0
 GBSPH_AV_VARYING_CD10 = 1
 GBSPH_AV_VARYING_MM97 = 2
@@ -50,7 +52,7 @@ class Config(C.Structure):
                 ("epsilon_h_particle", _f64), ("eos_kind", _u32), ("ext_kind", _u32),
                 ("cs0", _f64), ("eos_r0", _f64), ("eos_q", _f64), ("central_mass", _f64),
                 ("constant_G", _f64), ("av_kind", _u32), ("pad2", _u32), ("alpha_min", _f64),
-                ("alpha_max", _f64), ("sigma_decay", _f64)]
+                ("alpha_max", _f64), ("sigma_decay", _f64), ("mixed_tol", _f64)]
 
 
 class TimeState(C.Structure):
@@ -61,7 +63,8 @@ class StepLog(C.Structure):
     _fields_ = [("t", _f64), ("dt", _f64), ("next_dt", _f64), ("cfl_mult", _f64),
                 ("n_local", _u32), ("n_ghost", _u32), ("leaf_count", _u32), ("h_subcycles", _u32),
                 ("h_iterations", _u32), ("corrector_iters", _u32), ("cache_size", _u64),
-                ("eps_v", _f64), ("max_eps_h", _f64), ("elapsed_s", _f64), ("rate", _f64)]
+                ("eps_v", _f64), ("max_eps_h", _f64), ("elapsed_s", _f64), ("rate", _f64),
+                ("tier", _u32), ("tier_reruns", _u32), ("err_est_a", _f64), ("err_est_du", _f64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

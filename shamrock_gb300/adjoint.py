@@ -62,14 +62,16 @@ def _cot_struct(cot):
     return c
 
 
-def adjoint_step(model, start, t, dt, corrector_iters, cot):
+def adjoint_step(model, start, t, dt, corrector_iters, cot, tier=None):
     """One reverse step (gbsph_adjoint_step): updates the cotangent dict ``cot`` in place
-    from d/d(state after) to d/d(state before) and returns dL/d alpha_AV of the step."""
+    from d/d(state after) to d/d(state before) and returns dL/d alpha_AV of the step.
+    tier: the precision tier the forward step ran in (its log's "tier"; required when
+    the configured precision is the error-controlled "mixed")."""
     import torch
 
     lib = model._lib()
     p = _particles_of(start)
-    cfg = model._config_struct()
+    cfg = model._config_struct(tier)
     cs = _cot_struct(cot)
     g_alpha = C.c_double(0.0)
     torch.cuda.synchronize()
@@ -79,10 +81,10 @@ def adjoint_step(model, start, t, dt, corrector_iters, cot):
     return g_alpha.value
 
 
-def _step(model, t, dt):
+def _step(model, t, dt, tier=None):
     model.time = float(t)
     model.dt = float(dt)
-    return model.evolve_once()
+    return model.evolve_once(tier=tier)
 
 
 class _Rollout:
@@ -93,7 +95,7 @@ class _Rollout:
         self.n_steps = int(n_steps)
         self.k = max(1, int(checkpoint_every))
         self.dts = None if dts is None else [float(v) for v in dts]
-        self.records = []     # per step: (t, dt, corrector_iters)
+        self.records = []     # per step: (t, dt, corrector_iters, precision tier)
         self.checkpoints = {}  # step index -> state before that step
 
     def forward(self):
@@ -104,7 +106,7 @@ class _Rollout:
                 self.checkpoints[j] = _snapshot(m)
             dt = self.dts[j] if self.dts is not None else m.dt
             log = _step(m, t, dt)
-            self.records.append((t, dt, int(log["corrector_iters"])))
+            self.records.append((t, dt, int(log["corrector_iters"]), int(log["tier"])))
             t = t + dt
             if self.dts is None:
                 m.dt = log["next_dt"]
@@ -127,12 +129,12 @@ class _Rollout:
             seg = []
             for j in range(s0, s1):
                 seg.append(_snapshot(m))
-                t, dt, _ = self.records[j]
+                t, dt, _, tier = self.records[j]
                 if j + 1 < s1:
-                    _step(m, t, dt)
+                    _step(m, t, dt, tier)
             for j in reversed(range(s0, s1)):
-                t, dt, kk = self.records[j]
-                g_alpha += adjoint_step(m, seg[j - s0], t, dt, kk, cot)
+                t, dt, kk, tier = self.records[j]
+                g_alpha += adjoint_step(m, seg[j - s0], t, dt, kk, cot, tier)
         _restore(m, saved)
         m.time, m.dt, m.cfl_mult = saved_time
         torch.cuda.synchronize()

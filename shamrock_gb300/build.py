@@ -27,7 +27,7 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
 # FP64 units whose results are compared bit for bit with the oracle
 EXACT = {"tree.cu", "neigh.cu", "ghosts.cu", "sph64.cu", "scan.cu", "driver.cu"}
 # FP32-mixed pair kernels: approximate FP32 division / square root, denormals flushed
-FAST32 = {"sph_mixed.cu"}
+FAST32 = {"sph_mixed.cu", "sph_comp.cu"}
 
 
 def nvcc():

@@ -25,7 +25,7 @@ cudaError_t morton_codes_dev(Ctx &c, const f64 *x, const f64 *y, const f64 *z, u
                              int key_bits, void *out);
 cudaError_t export_boxes(Ctx &c, f64 *mn, f64 *mx, f64 *rint);
 
-unsigned long long g_kernel_launches = 0;
+std::atomic<unsigned long long> g_kernel_launches{0};
 
 int prof_begin(Ctx &c, int kind, u64 units) {
     size_t need = 2 * (c.prof.used + 1);
@@ -62,7 +62,7 @@ Ctx::~Ctx() {
                       &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
                       &owner, &leaf_thr, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
-                      &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2,
+                      &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2, &f_comp, &guard_state,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
                       &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &aext, &av_arank,
                       &av_alpha_rank, &av_alpha_upd, &av_diag};
@@ -143,6 +143,26 @@ __global__ void k_copy_state(u32 n, gbsph_vec3 x, gbsph_vec3 v, gbsph_vec3 a, co
     out[11 * n_ + i] = du[i];
 }
 
+// inverse of k_copy_state: SoA working copy -> the caller's (strided) fields
+__global__ void k_restore_state(u32 n, gbsph_vec3 x, gbsph_vec3 v, gbsph_vec3 a, f64 *h, f64 *u,
+                                f64 *du, const f64 *__restrict__ in) {
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t n_ = n;
+    x.x[(size_t) i * x.stride] = in[0 * n_ + i];
+    x.y[(size_t) i * x.stride] = in[1 * n_ + i];
+    x.z[(size_t) i * x.stride] = in[2 * n_ + i];
+    v.x[(size_t) i * v.stride] = in[3 * n_ + i];
+    v.y[(size_t) i * v.stride] = in[4 * n_ + i];
+    v.z[(size_t) i * v.stride] = in[5 * n_ + i];
+    a.x[(size_t) i * a.stride] = in[6 * n_ + i];
+    a.y[(size_t) i * a.stride] = in[7 * n_ + i];
+    a.z[(size_t) i * a.stride] = in[8 * n_ + i];
+    h[i]  = in[9 * n_ + i];
+    u[i]  = in[10 * n_ + i];
+    du[i] = in[11 * n_ + i];
+}
+
 } // namespace
 } // namespace gbsph
 
@@ -200,7 +220,7 @@ static const char *kProfNames[kProfCount] = {
 
 uint32_t gbsph_profile_kinds(void) { return kProfCount; }
 
-uint64_t gbsph_kernel_launches(void) { return g_kernel_launches; }
+uint64_t gbsph_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 int gbsph_set_cache_budget(gbsph_ctx *ctx, uint64_t bytes) {
     if (!ctx) return GBSPH_ERR_ARG;
@@ -586,16 +606,36 @@ int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double
 
 } // extern "C"
 
-// One step (Solver::evolve_once).  With a tape, exactly tape->forced_iters corrector
+// Estimated relative error of the FP32 tier's accelerations and du/dt on the last
+// corrector evaluation: the FP32 rounding of the pair terms, and of the h, rho, P, Omega
+// and u they are built from, errs in proportion to the summed term magnitudes, which the
+// derivatives pass accumulates per row; divided by the largest result.  The effective
+// relative error per unit of condition is 3e-7 for both: measured 1.4e-7 for the forces
+// on the 64^3 sound wave (condition 3.2e4, error 4.4e-3), 6e-8 for du/dt there
+// (condition 4.4e3, error 2.6e-4) and 1.8e-7 for du/dt on a Sedov blast (condition 1.3,
+// error 2.4e-7: the rounding of well-conditioned FP32 sums).  A field that vanishes
+// while its terms do not is taken as unbounded error.
+static constexpr f64 kErrEffA  = 3e-7;
+static constexpr f64 kErrEffDu = 3e-7;
+static f64 err_estimate(f64 eff, u64 sum_bits, u64 max_bits) {
+    const f64 s = ordered_to_f64(sum_bits), m = ordered_to_f64(max_bits);
+    if (!(s > 0)) return 0;
+    if (!(m > 0)) return std::numeric_limits<f64>::infinity();
+    return eff * s / m;
+}
+
+// One step (Solver::evolve_once) in one precision tier (GBSPH_FP64, GBSPH_MIXED or
+// GBSPH_MIXED_COMPENSATED).  With a tape, exactly tape->forced_iters corrector
 // evaluations run and the velocity / energy before each is recorded.
-static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
-                       gbsph_time_state *ts, gbsph_step_log *log, StepTape *tape) {
+static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
+                       gbsph_time_state *ts, gbsph_step_log *log, StepTape *tape, u32 tier) {
     Ctx &c = ctx->c;
     REQUIRE_ARG(p && cfg && ts, "null argument");
     REQUIRE_ARG(p->n > 0, "empty patch");
     REQUIRE_ARG(cfg->pmass > 0,
                 "invalid gpart_mass, this configuration can not converge (Solver.cpp:1096-1102)");
-    REQUIRE_ARG(cfg->precision == GBSPH_FP64 || cfg->precision == GBSPH_MIXED, "unknown precision");
+    REQUIRE_ARG(tier == GBSPH_FP64 || tier == GBSPH_MIXED || tier == GBSPH_MIXED_COMPENSATED,
+                "unknown precision");
     REQUIRE_ARG(p->xyz.stride == p->vxyz.stride && p->xyz.stride == p->axyz.stride,
                 "xyz, vxyz and axyz must share one element stride");
     REQUIRE_ARG(cfg->eos_kind == GBSPH_EOS_ADIABATIC || cfg->eos_kind == GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07,
@@ -618,7 +658,8 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     cudaStream_t s = c.stream;
     const u32 n    = p->n;
     const f64 dt   = ts->dt;
-    const bool mixed = cfg->precision == GBSPH_MIXED;
+    const bool mixed = tier != GBSPH_FP64;
+    const bool comp  = tier == GBSPH_MIXED_COMPENSATED;
     LocalFields lf{p->xyz.x,  p->xyz.y,  p->xyz.z,  p->vxyz.x, p->vxyz.y,  p->vxyz.z,
                    p->axyz.x, p->axyz.y, p->axyz.z, p->xyz.stride, p->hpart, p->uint, p->duint};
     gbsph_step_log lg;
@@ -725,9 +766,17 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     lg.leaf_count  = c.leaf_count;
     lg.cache_size  = c.csr_total;
     u32 N          = n + c.n_ghost;
-    if (mixed) CU(omega_mixed(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>()));
-    else CU(omega64(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>(),
-                    c.row_local.as<u32>()));
+    if (comp) {
+        // compensated tier: h finished by one double-float Newton step, Omega at it
+        CU(dens_polish_df(c, rs, c.h_old_row.as<f64>(), c.hnew_row.as<f64>(), c.eps_row.as<f64>(),
+                          cfg->htol_up_coarse, cfg->htol_up_fine, c.omega_local.as<f64>()));
+        CU(scatter_rows(c, n, c.hnew_row.as<f64>(), lf.h));
+    } else if (mixed) {
+        CU(omega_mixed(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>()));
+    } else {
+        CU(omega64(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>(),
+                   c.row_local.as<u32>()));
+    }
     if (p->omega)
         CU(cudaMemcpyAsync(p->omega, c.omega_local.p, 8 * (size_t) n, cudaMemcpyDeviceToDevice, s));
 
@@ -753,7 +802,8 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             return fail(ctx, GBSPH_ERR_NOT_CONVERGED,
                         "the corrector has made over 50 loops, either their is a bug, either you "
                         "are using a dt that is too large");
-        if (mixed) CU(gather_stage_mixed(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos, cd10));
+        if (mixed)
+            CU(gather_stage_mixed(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos, cd10, comp));
         else CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));
         hs.alpha = nullptr;
         if (cd10) {
@@ -810,9 +860,14 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         { k_reset_corrector<<<1, 1, 0, s>>>(dsc); GBSPH_COUNTED; }
         f64 C_cour  = cfg->cfl_cour * ts->cfl_mult;
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
-        if (mixed)
+        // the error estimate of the mixed tiers comes from the step's first evaluation
+        const bool cond = corr_iters == 0;
+        if (comp)
+            CU(derivs_step_comp(c, rs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
+                                dt / 2, C_cour, C_force, lf, ext, cd10, cond));
+        else if (mixed)
             CU(derivs_step_mixed(c, rs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
-                                 dt / 2, C_cour, C_force, lf, ext, cd10));
+                                 dt / 2, C_cour, C_force, lf, ext, cd10, cond));
         else
             CU(derivs_step64(c, rs, hs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
                              dt / 2, C_cour, C_force, lf, ext));
@@ -856,9 +911,94 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     lg.cfl_mult        = ts->cfl_mult;
     lg.elapsed_s       = elapsed;
     lg.rate            = elapsed > 0 ? f64(n) / elapsed : 0;
+    lg.tier            = tier;
+    if (mixed) {
+        lg.err_est_a  = err_estimate(kErrEffA, c.h_scalars->cond_fa, c.h_scalars->cond_a);
+        lg.err_est_du = err_estimate(kErrEffDu, c.h_scalars->cond_fu, c.h_scalars->cond_du);
+    }
     if (log) *log = lg;
     if (!converged) ctx->c.err = "the h iterator is not converged after the maximum number of "
                                  "sub-cycles (step continued, as the reference does)";
+    return GBSPH_OK;
+}
+
+// Start state of a step that may be recomputed: the caller's x, v, a, h, u, du (and the
+// varying viscosity's alpha_AV and sound speed), SoA in c.guard_state.
+static int save_state(gbsph_ctx *ctx, const gbsph_particles *p, bool av) {
+    Ctx &c = ctx->c;
+    const u32 n = p->n;
+    const size_t n_ = n;
+    CU(c.guard_state.ensure(sizeof(f64) * 14 * n_, c.stream));
+    f64 *S = c.guard_state.as<f64>();
+    { k_copy_state<<<div_up(n, 256), 256, 0, c.stream>>>(n, p->xyz, p->vxyz, p->axyz, p->hpart,
+                                                       p->uint, p->duint, S); GBSPH_COUNTED; }
+    CU(cudaGetLastError());
+    if (av) {
+        CU(cudaMemcpyAsync(S + 12 * n_, p->alpha_AV, 8 * n_, cudaMemcpyDeviceToDevice, c.stream));
+        CU(cudaMemcpyAsync(S + 13 * n_, p->soundspeed, 8 * n_, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    return GBSPH_OK;
+}
+
+static int restore_state(gbsph_ctx *ctx, const gbsph_particles *p, bool av) {
+    Ctx &c = ctx->c;
+    const u32 n = p->n;
+    const size_t n_ = n;
+    const f64 *S = c.guard_state.as<f64>();
+    { k_restore_state<<<div_up(n, 256), 256, 0, c.stream>>>(n, p->xyz, p->vxyz, p->axyz, p->hpart,
+                                                          p->uint, p->duint, S); GBSPH_COUNTED; }
+    CU(cudaGetLastError());
+    if (av) {
+        CU(cudaMemcpyAsync(p->alpha_AV, S + 12 * n_, 8 * n_, cudaMemcpyDeviceToDevice, c.stream));
+        CU(cudaMemcpyAsync(p->soundspeed, S + 13 * n_, 8 * n_, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    return GBSPH_OK;
+}
+
+// One step in the configured precision; GBSPH_MIXED_GUARDED picks the tier (see gbsph.h).
+static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_config *cfg,
+                       gbsph_time_state *ts, gbsph_step_log *log, StepTape *tape) {
+    REQUIRE_ARG(p && cfg && ts, "null argument");
+    if (cfg->precision != GBSPH_MIXED_GUARDED)
+        return evolve_tier(ctx, p, cfg, ts, log, tape, cfg->precision);
+    REQUIRE_ARG(!tape, "the adjoint step recomputes the forward step in the tier it ran in "
+                       "(gbsph_step_log.tier), not in GBSPH_MIXED_GUARDED");
+    REQUIRE_ARG(p->n > 0, "empty patch");
+    Ctx &c = ctx->c;
+    auto t0        = std::chrono::steady_clock::now();
+    const f64 tol  = cfg->mixed_tol > 0 ? cfg->mixed_tol : 1e-5;
+    const bool av  = cfg->av_kind != GBSPH_AV_CONSTANT && p->alpha_AV && p->soundspeed;
+    u32 tier       = c.guard_tier == GBSPH_MIXED_COMPENSATED ? GBSPH_MIXED_COMPENSATED : GBSPH_MIXED;
+    const gbsph_time_state ts0 = *ts;
+    if (tier == GBSPH_MIXED) {
+        int st = save_state(ctx, p, av);
+        if (st != GBSPH_OK) return st;
+    }
+    gbsph_step_log lg;
+    std::memset(&lg, 0, sizeof(lg));
+    int st = evolve_tier(ctx, p, cfg, ts, &lg, nullptr, tier);
+    if (st != GBSPH_OK) return st;
+    f64 est = std::max(lg.err_est_a, lg.err_est_du);
+    u32 reruns = 0;
+    if (tier == GBSPH_MIXED && !(est <= tol)) {
+        // the FP32 tier cannot be trusted with this state: redo the step compensated
+        st = restore_state(ctx, p, av);
+        if (st != GBSPH_OK) return st;
+        *ts = ts0;
+        st = evolve_tier(ctx, p, cfg, ts, &lg, nullptr, GBSPH_MIXED_COMPENSATED);
+        if (st != GBSPH_OK) return st;
+        reruns = 1;
+        tier   = GBSPH_MIXED_COMPENSATED;
+        est    = std::max(lg.err_est_a, lg.err_est_du);
+    }
+    // the next step starts in the tier this one needed, and returns to FP32 once the
+    // estimate is well inside the tolerance
+    c.guard_tier    = (tier == GBSPH_MIXED_COMPENSATED && !(est <= tol / 4)) ? GBSPH_MIXED_COMPENSATED
+                                                                            : GBSPH_MIXED;
+    lg.tier_reruns  = reruns;
+    lg.elapsed_s    = std::chrono::duration<f64>(std::chrono::steady_clock::now() - t0).count();
+    lg.rate         = lg.elapsed_s > 0 ? f64(p->n) / lg.elapsed_s : 0;
+    if (log) *log = lg;
     return GBSPH_OK;
 }
 
@@ -932,8 +1072,9 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     cs.vs   = cot->gx.stride;
     Scalars *dsc = c.d_scalars.as<Scalars>();
     CU(cudaMemsetAsync(&dsc->g_alpha, 0, sizeof(f64), s));
+    // FP32 reverse pass after either mixed tier's recompute, FP64 after the FP64 one
     CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), tape, ap, cs, &dsc->g_alpha,
-                        cfg->precision == GBSPH_MIXED));
+                        cfg->precision != GBSPH_FP64));
     CU(sync_scalars(c));
     if (g_alpha_av) *g_alpha_av += c.h_scalars->g_alpha;
     return GBSPH_OK;

@@ -29,6 +29,10 @@ struct Scalars {
     u64 dt_min;        // ordered-u64 min of per-particle CFL dt
     u64 n_unconverged; // particles whose per-thread iteration cap was hit
     u64 csr_entries;   // stage-2 entries of the one-pass cache build
+    u64 cond_fa;       // ordered-u64 max over rows of the force condition sum (mixed)
+    u64 cond_fu;       // ordered-u64 max of the du/dt condition sum
+    u64 cond_a;        // ordered-u64 max |bare hydro force sum|
+    u64 cond_du;       // ordered-u64 max |bare du/dt sum|
     f64 sum_v2;        // sum of |v|^2 after the corrector
     f64 g_alpha;       // adjoint: dL / d alpha_AV of one step
     f64 cons[8];       // conservation totals (momentum, energies)
@@ -143,8 +147,12 @@ struct Ctx {
 
     // ---- per-step fields in rank order (corrector phase)
     DevBuf su, svx, svy, svz, som, sP, scs, sh2;
-    // mixed precision staging (rank order)
-    DevBuf f_pos, f_anchor, f_aux0, f_aux1, f_aux2;
+    // mixed precision staging (rank order); f_comp: the compensated tier's extra records
+    DevBuf f_pos, f_anchor, f_aux0, f_aux1, f_aux2, f_comp;
+    // error-controlled mixed precision: the tier the next step starts in (1 FP32 pair
+    // arithmetic, 2 compensated) and the start state a step is recomputed from
+    u32 guard_tier = 1;
+    DevBuf guard_state;
 
     // ---- per-row / per-local work arrays
     DevBuf h_old_row, eps_row, omega_local, a_old, du_old, hnew_row, omega_row;

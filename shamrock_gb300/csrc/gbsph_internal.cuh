@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 typedef uint8_t u8;
@@ -35,9 +36,10 @@ typedef float f32;
 namespace gbsph {
 
 // Process-wide count of kernel launches issued by this library (every launch site is
-// followed by GBSPH_COUNTED); read through gbsph_kernel_launches().
-extern unsigned long long g_kernel_launches;
-#define GBSPH_COUNTED (++::gbsph::g_kernel_launches)
+// followed by GBSPH_COUNTED); read through gbsph_kernel_launches().  Atomic: contexts
+// on different host threads, and the context-free entry point, count into it at once.
+extern std::atomic<unsigned long long> g_kernel_launches;
+#define GBSPH_COUNTED (::gbsph::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
 
 // ------------------------------------------------------------------ constants
 // M4 cubic spline, shammath/include/shammath/sphkernels.hpp:29-72

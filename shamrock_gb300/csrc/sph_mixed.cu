@@ -19,83 +19,12 @@
 // rho_sum / rho_h and h (d rho / dh) / rho_h, and the CFL step runs in FP32.  FP64 stays
 // on the state (h, x, v, u, a) and on pressure, whose hi/lo pair carries it beyond FP32.
 
-#include "sph_mixed.cuh"
-#include "split64.cuh"
-
-#include <cuda_bf16.h>
+#include "mixed_common.cuh"
 
 namespace gbsph {
 
 namespace {
 
-constexpr float kNorm3dF = 0.318309886183790671538f; // 1/pi
-
-__device__ __forceinline__ float m4_f32(float q) {
-    float t1 = 2.f - q, t2 = 1.f - q;
-    t1 = t1 * t1 * t1 * 0.25f;
-    t2 = -(t2 * t2 * t2);
-    return q < 1.f ? t1 + t2 : (q < 2.f ? t1 : 0.f);
-}
-__device__ __forceinline__ float m4_df32(float q) {
-    return q < 1.f ? (-3.f * q + 2.25f * q * q) : (q < 2.f ? (-3.f + 3.f * q - 0.75f * q * q) : 0.f);
-}
-// sqrt(x) for x >= 0 from the hardware reciprocal square root (about 2 ulp; the pair
-// loops need 1e-5, and the correctly rounded sqrtf costs several more instructions per
-// pair); 0 for x = 0
-__device__ __forceinline__ float sqrt_approx(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
-__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
-    float y = v - c;
-    float t = s + y;
-    c       = (t - s) - y;
-    s       = t;
-}
-__device__ __forceinline__ float hi32(f64 v) { return __double2float_rn(v); }
-__device__ __forceinline__ float lo32(f64 v) { return __double2float_rn(v - (f64) __double2float_rn(v)); }
-// 1/v from the FP32 reciprocal refined by one FP64 Newton step (relative error ~1e-14,
-// so its FP32 rounding is the correctly rounded 1/v but for rare ties); plain FP64
-// division where the FP32 reciprocal leaves the normal range
-__device__ __forceinline__ f64 rcp64(f64 v) {
-    const float y0 = __frcp_rn(__double2float_rn(v));
-    if (!(fabsf(y0) < 3.0e38f && fabsf(y0) > 1.0e-37f)) return 1.0 / v;
-    const f64 y = (f64) y0;
-    return y * (2.0 - v * y);
-}
-// kNorm3d / hfact^3: rho_sum / rho_h = kC sum f(q), h (d rho/dh) / rho_h = -kC sum (3f + q f')
-constexpr float kDensRatio = (float) (kNorm3d / (kHfact * kHfact * kHfact));
-
-// Two residuals in one 32-bit word as bfloat16 (8 exponent bits: the range of a float,
-// so no residual underflows): with hi = fl32(v) the pair hi + bf16(lo) carries v to
-// about 2^-33 relative.
-__device__ __forceinline__ float pack_bf16x2(float a, float b) {
-    u32 ha = __bfloat16_as_ushort(__float2bfloat16_rn(a));
-    u32 hb = __bfloat16_as_ushort(__float2bfloat16_rn(b));
-    return __uint_as_float((ha << 16) | hb);
-}
-__device__ __forceinline__ float bf_hi(float w) { return __uint_as_float(__float_as_uint(w) & 0xffff0000u); }
-__device__ __forceinline__ float bf_lo(float w) { return __uint_as_float(__float_as_uint(w) << 16); }
-
-__device__ __forceinline__ f64 rho_h64(f64 m, f64 h) {
-    return m * (kHfact / h) * (kHfact / h) * (kHfact / h);
-}
-
-// Four CSR entries from k on as a uint4, slots at or past k1 set to `pad`.  vec: the row
-// is padded to 4-entry boundaries (library cache) and is read with one 128-bit load.
-__device__ __forceinline__ uint4 load_entries(const u32 *__restrict__ ent, u32 k, u32 k1, bool vec,
-                                              u32 pad) {
-    uint4 v;
-    if (vec) {
-        v = __ldg((const uint4 *) (ent + k));
-    } else {
-        v.x = __ldg(&ent[k]);
-        v.y = (k + 1 < k1) ? __ldg(&ent[k + 1]) : pad;
-        v.z = (k + 2 < k1) ? __ldg(&ent[k + 2]) : pad;
-        v.w = (k + 3 < k1) ? __ldg(&ent[k + 3]) : pad;
-    }
-    if (k + 1 >= k1) v.y = pad;
-    if (k + 2 >= k1) v.z = pad;
-    if (k + 3 >= k1) v.w = pad;
-    return v;
-}
 
 // B.w carries fl32 of the neighbour-cache threshold ((h htol)^2) R^2 (computed in FP64
 // in the reference's order) for the FP32 pre-test of the cache build; the corrector
@@ -169,6 +98,7 @@ struct StageEos {
     float gg;       // gamma (gamma - 1)
     float inv_r0sq; // 1 / r0^2
     float cs0sq, mq;
+    f64 inv_r0sq64, cs0sq64, mq64; // the same in FP64 (compensated tier)
 };
 
 __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
@@ -177,7 +107,7 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
                                      const f64 *__restrict__ sx, const f64 *__restrict__ sy,
                                      const f64 *__restrict__ sz, float4 *__restrict__ P,
                                      float4 *__restrict__ H, f64 *__restrict__ h_rank,
-                                     StageAV av) {
+                                     StageAV av, float4 *__restrict__ E) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
     u32 id  = sort_index[r];
@@ -197,7 +127,13 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
     const f64 rho      = eos.mh3 * hinv * hinv * hinv;
     f64 Pr;
     float cs;
-    if (eos.kind == 1) {
+    if (eos.kind == 1 && E) {
+        // compensated tier: the pressure to FP64 accuracy
+        const f64 Rsq   = sx[r] * sx[r] + sy[r] * sy[r] + sz[r] * sz[r];
+        const f64 cs_sq = eos.cs0sq64 * pow(Rsq * eos.inv_r0sq64, eos.mq64);
+        Pr              = cs_sq * rho;
+        cs              = (float) sqrt(cs_sq);
+    } else if (eos.kind == 1) {
         float ratio = (xh * xh + yh * yh + zh * zh) * eos.inv_r0sq;
         float cs_sq = eos.cs0sq * powf(ratio, eos.mq);
         Pr          = (f64) cs_sq * rho;
@@ -220,6 +156,19 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
         av.V[p2 + 1] = make_float4(__double2float_rn(av.ay[iv]), __double2float_rn(av.az[iv]),
                                    pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, 0.f));
         av.cs_rank[r] = cs;
+    }
+    if (E) {
+        // X = P / (rho^2 Omega) (zero where the reference's inv_sat_zero gives zero), the
+        // residuals of 1/h, P and u, and 1/h^4, as double-floats
+        const f64 X = (sub != 0 && sub == sub) ? Pr * rcp64(sub) : 0.;
+        float Xh, Xl, h4h, h4l;
+        split64(X, Xh, Xl);
+        const f64 hinv2 = hinv * hinv;
+        split64(hinv2 * hinv2, h4h, h4l);
+        const float hinv_lo = __double2float_rn(hinv - (f64) hinv_f);
+        const float u_lo    = __double2float_rn(uu - (f64) __double2float_rn(uu));
+        E[p2]     = make_float4(Xh, Xl, hinv_lo, Pl);
+        E[p2 + 1] = make_float4(u_lo, h4h, h4l, 0.f);
     }
 }
 
@@ -327,10 +276,6 @@ __global__ void __launch_bounds__(256) k_omega_mixed(RowSpace rs, MixedSpace ms,
     omega_local[rs.row_local ? rs.row_local[t] : t] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
 }
 
-struct MixedParams {
-    float alpha_u, alpha_AV, beta_AV;
-    float mh3; // m hfact^3: rho = mh3 / h^3
-};
 
 // FP32 pair loop of the constant-AV derivatives; returns the bare sums
 //   F = sum (ca Fa + cb Fb) r_hat   (acceleration = -m F)
@@ -341,9 +286,16 @@ struct MixedParams {
 // makes padding a partial batch of four with the row's own index harmless.
 // cs_rank (varying viscosity): the records' c_s lane holds alpha c_s, p.alpha_AV is 1,
 // and the plain c_s of the row for the v_sig maximum comes from cs_rank.
+// Condition sums for the error estimate of the step (unused by the module kernels):
+//   sa = sum |AVP_a c1a F_a + AVP_b c1b F_b|, the magnitudes of the pair forces whose sum
+//        is F (their FP32 rounding, and that of the h behind them, errs in proportion);
+//   su = sum |P-term| + |conductivity coefficient| (|u_a| + |u_b|), the du/dt terms with
+//        the energy difference replaced by the magnitudes it is taken from.
+template<bool COND = false>
 __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSpace &ms, u32 a,
                                                u32 k0, u32 k1, const MixedParams &p, float &Fx,
                                                float &Fy, float &Fz, float &U, float &vsig_max,
+                                               float &sa, float &su,
                                                const float *__restrict__ cs_rank = nullptr) {
     const bool vec = rs.row_rank != nullptr;
     const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
@@ -359,6 +311,8 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
     float cx = 0.f, cy = 0.f, cz = 0.f, cu = 0.f;
     Fx = Fy = Fz = U = 0.f;
     vsig_max = 0.f;
+    sa = su = 0.f;
+    const float abs_ua = fabsf(u_a);
     uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, vec, a) : make_uint4(a, a, a, a);
     for (u32 k = k0; k < k1; k += 4) {
         // both records of all four neighbours in one round trip, next entries behind them
@@ -402,11 +356,20 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
             float qa = fmaxf(-0.5f * rho_a * vsig_a * vr, 0.f);
             float qb = fmaxf(-0.5f * rho_b * vsig_b * vr, 0.f);
             float AVPa = P_a + qa, AVPb = P_b + qb;
-            float f    = (AVPa * c1a * Fa + AVPb * c1b * Fb) * rinv;
+            float pf   = AVPa * c1a * Fa + AVPb * c1b * Fb;
+            float f    = pf * rinv;
             bx += f * dx;
             by += f * dy;
             bz += f * dz;
-            bu += AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - hb[j].a.w) * (Fa * c2a + Fb * c2b);
+            if (COND) {
+                const float tp = AVPa * c1a * Fa * vr;
+                const float tc = 0.5f * p.alpha_u * vsig_u * (Fa * c2a + Fb * c2b);
+                bu += tp + tc * (u_a - hb[j].a.w);
+                sa += fabsf(pf);
+                su += fabsf(tp) + fabsf(tc) * (abs_ua + fabsf(hb[j].a.w));
+            } else {
+                bu += AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - hb[j].a.w) * (Fa * c2a + Fb * c2b);
+            }
             vsig_max = fmaxf(vsig_max, cs_sig + 2.f * avr);
         }
         kahan_add(Fx, cx, bx);
@@ -424,8 +387,8 @@ __global__ void __launch_bounds__(128) k_derivs_mixed(RowSpace rs, MixedSpace ms
     if (t >= rs.n) return;
     u32 a  = rs.row_rank ? rs.row_rank[t] : t;
     u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
-    float Fx, Fy, Fz, U, vm;
-    derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm);
+    float Fx, Fy, Fz, U, vm, sa, su;
+    derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm, sa, su);
     ax[t] = -pmass * (f64) Fx;
     ay[t] = -pmass * (f64) Fy;
     az[t] = -pmass * (f64) Fz;
@@ -433,6 +396,9 @@ __global__ void __launch_bounds__(128) k_derivs_mixed(RowSpace rs, MixedSpace ms
     if (vsig) vsig[t] = (f64) vm;
 }
 
+// COND: also the condition sums of the step's error estimate (first corrector
+// evaluation of a step; the others skip their cost)
+template<bool COND>
 __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpace ms,
                                                            MixedParams p, f64 pmass,
                                                            const f64 *__restrict__ h_rank, f64 hdt,
@@ -442,11 +408,18 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     u64 ev2 = 0, dtm = ~0ull;
     float v2 = 0.f;
+    float c_fa = 0.f, c_fu = 0.f, c_a = 0.f, c_du = 0.f; // condition sums and magnitudes
     if (t < rs.n) {
         u32 a  = rs.row_rank[t];
         u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
-        float Fx, Fy, Fz, U, vm;
-        derivs_row_f32(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm, cs_rank);
+        float Fx, Fy, Fz, U, vm, sa, su;
+        derivs_row_f32<COND>(rs, ms, a, k0, k1, p, Fx, Fy, Fz, U, vm, sa, su, cs_rank);
+        if (COND) {
+            c_fa = sa;
+            c_fu = su;
+            c_a  = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
+            c_du = fabsf(U);
+        }
         f64 fx = -pmass * (f64) Fx, fy = -pmass * (f64) Fy, fz = -pmass * (f64) Fz;
         f64 tdu = pmass * (f64) U;
         u32 i     = rs.row_local[t];
@@ -483,6 +456,7 @@ __global__ void __launch_bounds__(128) k_derivs_step_mixed(RowSpace rs, MixedSpa
     ev2 = block_reduce(ev2, OpMaxU64{}, 0ull);
     dtm = block_reduce(dtm, OpMinU64{}, ~0ull);
     v2  = block_reduce(v2, OpAddF32{}, 0.f);
+    if (COND) cond_reduce(sc, c_fa, c_fu, c_a, c_du);
     if (threadIdx.x == 0) {
         atomicMax((unsigned long long *) &sc->epsv2_max, (unsigned long long) ev2);
         atomicMin((unsigned long long *) &sc->dt_min, (unsigned long long) dtm);
@@ -625,10 +599,6 @@ __global__ void k_cs_to_local(u32 n, const u32 *__restrict__ row_rank,
     dst[row_local[t]] = (f64) cs_rank[row_rank[t]];
 }
 
-MixedParams mixed_params(f64 pmass, f64 alpha_u, f64 alpha_AV, f64 beta_AV) {
-    f64 mh3 = pmass * kHfact * kHfact * kHfact;
-    return MixedParams{(float) alpha_u, (float) alpha_AV, (float) beta_AV, (float) mh3};
-}
 
 // f_pos holds 2N float4 (position records), f_aux0 2N float4 (hydro records)
 MixedSpace mixed_space(Ctx &c, u32 N) {
@@ -674,7 +644,13 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
 
 cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
                                const f64 *omega_local, f64 pmass, const EosParams &eos,
-                               bool varying_av) {
+                               bool varying_av, bool compensated) {
+    float4 *E = nullptr;
+    if (compensated) {
+        cudaError_t e = c.f_comp.ensure(2 * sizeof(float4) * (size_t) N, c.stream);
+        if (e != cudaSuccess) return e;
+        E = c.f_comp.as<float4>();
+    }
     StageAV av{lf.ax, lf.ay, lf.az, nullptr, nullptr};
     if (varying_av) {
         cudaError_t e;
@@ -685,26 +661,28 @@ cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf
     }
     StageEos se{eos.kind, eos.gamma - 1, pmass * kHfact * kHfact * kHfact,
                 (float) (eos.gamma * (eos.gamma - 1)), (float) (1.0 / (eos.r0 * eos.r0)),
-                (float) (eos.cs0 * eos.cs0), (float) -eos.q};
+                (float) (eos.cs0 * eos.cs0), (float) -eos.q, 1.0 / (eos.r0 * eos.r0),
+                eos.cs0 * eos.cs0, -eos.q};
     ProfScope ps(c, kProfGatherEos, N);
     { k_gather_stage_mixed<<<div_up(N, 256), 256, 0, c.stream>>>(
         c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf, omega_local, pmass, se,
         c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(), c.f_pos.as<float4>(),
-        c.f_aux0.as<float4>(), c.sh2.as<f64>(), av); GBSPH_COUNTED; }
+        c.f_aux0.as<float4>(), c.sh2.as<f64>(), av, E); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
                               f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
-                              const LocalFields &lf, const ExtAccel &ext, bool varying_av) {
+                              const LocalFields &lf, const ExtAccel &ext, bool varying_av,
+                              bool cond) {
     MixedSpace ms = mixed_space(c, c.n_obj);
     MixedParams p = mixed_params(pmass, alpha_u, varying_av ? 1.0 : alpha_AV, beta_AV);
     const float *cs_rank = varying_av ? c.f_aux2.as<float>() : nullptr;
     ProfScope ps(c, kProfDerivs, rs.n);
-    { k_derivs_step_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, c.sh2.as<f64>(), hdt, C_cour,
-                                                                 C_force, lf, ext,
-                                                                 c.d_scalars.as<Scalars>(),
-                                                                 cs_rank); GBSPH_COUNTED; }
+    auto kern = cond ? k_derivs_step_mixed<true> : k_derivs_step_mixed<false>;
+    { kern<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, ms, p, pmass, c.sh2.as<f64>(), hdt, C_cour,
+                                                    C_force, lf, ext, c.d_scalars.as<Scalars>(),
+                                                    cs_rank); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 
@@ -761,9 +739,6 @@ constexpr u32 kNoAllocMaxMerged = 1u << 16;
 // loads the library and kept until the process exits.
 static __device__ __align__(256) float4 g_noalloc_staging[4 * kNoAllocMaxMerged];
 
-constexpr int kNoAllocMaxDevices = 64;
-float4 *g_noalloc_base[kNoAllocMaxDevices] = {};
-
 } // namespace
 
 } // namespace gbsph
@@ -778,18 +753,17 @@ extern "C" int gbsph_derivs_constAV_mixed_noalloc(
     if (n_merged > kNoAllocMaxMerged) return GBSPH_ERR_CAPACITY; // beyond the fixed staging
     if (n_local > n_merged) return GBSPH_ERR_ARG;
     if (n_local == 0) return GBSPH_OK;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return GBSPH_ERR_CUDA;
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return GBSPH_ERR_ARG;
-    // Set-up, once per device, with that device current: the array's name in host code
-    // is only a host-side handle, the kernels need its device address.
-    if (!g_noalloc_base[dev]) {
-        void *p       = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_staging);
-        if (e != cudaSuccess || !p) return GBSPH_ERR_CUDA;
-        g_noalloc_base[dev] = (float4 *) p;
-    }
-    float4 *b     = g_noalloc_base[dev];
+    // Set-up, on every call, with the caller's device current: in host code the array's
+    // name is only a host-side handle, the kernels need its device address.  The address
+    // belongs to the module loaded in the current context, so it is looked up each time
+    // (a table lookup once the module is loaded) rather than cached per device: a cached
+    // address would go stale after cudaDeviceReset or under another driver-API context on
+    // the same device, and the lookup needs no host-side shared state.  The first call in
+    // a context loads the module, which must not happen inside a stream capture.
+    void *base    = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_staging);
+    if (e != cudaSuccess || !base) return GBSPH_ERR_CUDA;
+    float4 *b     = (float4 *) base;
     u32 N         = n_merged;
     // N position records (2N float4) then N hydro records (2N float4)
     MixedSpace ms{b, b + 2 * (size_t) N};

@@ -33,13 +33,18 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
 // then the fused derivatives step, which reads the records, c.sh2 and the caller's
 // local fields
 // varying_av: also stage FP32 acceleration records and the plain c_s per rank
+// compensated: also the compensated tier's records (c.f_comp, 2 float4 per rank:
+// {X_hi, X_lo, (1/h)_lo, P_lo} {u_lo, (1/h^4)_hi, (1/h^4)_lo, 0} with
+// X = P / (rho^2 Omega)), and the LP07 power in FP64
 cudaError_t gather_stage_mixed(Ctx &c, u32 N, u32 n_local, const LocalFields &lf,
                                const f64 *omega_local, f64 pmass, const EosParams &eos,
-                               bool varying_av = false);
+                               bool varying_av = false, bool compensated = false);
 // varying_av: per-particle alpha folded into the records' c_s lane (stage_alpha_mixed)
+// cond: also accumulate the condition sums of the error estimate (Scalars::cond_*)
 cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
                               f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force,
-                              const LocalFields &lf, const ExtAccel &ext, bool varying_av = false);
+                              const LocalFields &lf, const ExtAccel &ext, bool varying_av = false,
+                              bool cond = false);
 // varying viscosity: div v, curl v, d(div v)/dt per row (outputs by local id), after
 // gather_stage_mixed(..., true); alpha of the local particles into the records; the
 // staged plain c_s back to local order
@@ -47,6 +52,15 @@ cudaError_t velgrad_mixed(Ctx &c, const RowSpace &rs, const f64 *omega_local, f6
                           f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv);
 cudaError_t stage_alpha_mixed(Ctx &c, u32 N, u32 n_local, const f64 *alpha_local);
 cudaError_t cs_to_local_mixed(Ctx &c, u32 n, f64 *dst);
+// sph_comp.cu, the compensated tier: one double-float Newton step of h per row (rows
+// whose iteration did not converge keep their h) and Omega at the result (by local id),
+// from the position records of stage_positions_mixed
+cudaError_t dens_polish_df(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_row, const f64 *eps,
+                           f64 h_evol_max, f64 h_evol_iter_max, f64 *omega_local);
+// compensated derivatives step (after gather_stage_mixed(..., compensated = true))
+cudaError_t derivs_step_comp(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u, f64 alpha_AV,
+                             f64 beta_AV, f64 hdt, f64 C_cour, f64 C_force, const LocalFields &lf,
+                             const ExtAccel &ext, bool varying_av = false, bool cond = false);
 cudaError_t derivs_mixed_module(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 pmass,
                                 f64 alpha_u, f64 alpha_AV, f64 beta_AV, f64 *ax, f64 *ay, f64 *az,
                                 f64 *du, f64 *vsig);

@@ -20,6 +20,10 @@ import numpy as np
 
 from . import _lib as L
 
+# SolverConfig.precision -> gbsph_config.precision
+PRECISION_CODES = {"fp64": L.GBSPH_FP64, "mixed": L.GBSPH_MIXED_GUARDED,
+                   "mixed_fp32": L.GBSPH_MIXED, "mixed_compensated": L.GBSPH_MIXED_COMPENSATED}
+
 FIELDS_VEC = ("xyz", "vxyz", "axyz")
 FIELDS_SCAL = ("hpart", "uint", "duint")
 # fields of the varying (CD10) viscosity: state alpha_AV and soundspeed, diagnostics
@@ -64,6 +68,7 @@ class SolverConfig:
         self.h_iter_per_subcycles = 50
         self.h_max_subcycles_count = 100
         self.precision = "fp64"
+        self.mixed_tol = 0.0  # 0: the library's 1e-5
         self.ext_forces = []
         # G without a unit system is the SI value, as the reference's get_constant_G
         self.constant_G = G_SI
@@ -149,11 +154,19 @@ class SolverConfig:
         together with epsilon_h converges h further (GB300 extension)."""
         self.epsilon_h_particle = float(eps)
 
-    def set_precision(self, precision):
-        """"fp64" (bit-identical to the FP64 oracle) or "mixed" (FP32 pair arithmetic)."""
-        if precision not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+    PRECISIONS = ("fp64", "mixed", "mixed_fp32", "mixed_compensated")
+
+    def set_precision(self, precision, tol=None):
+        """"fp64": bit-identical to the FP64 oracle.  "mixed": error-controlled mixed
+        precision, FP32 pair arithmetic where the step's error estimate stays within
+        ``tol`` (default 1e-5 of the largest acceleration and du/dt), the compensated
+        tier where it does not.  "mixed_fp32": FP32 pair arithmetic without the control.
+        "mixed_compensated": the compensated tier on every step (GB300 extensions)."""
+        if precision not in self.PRECISIONS:
+            raise ValueError("precision must be one of " + ", ".join(self.PRECISIONS))
         self.precision = precision
+        if tol is not None:
+            self.mixed_tol = float(tol)
 
     def has_field_alphaAV(self):
         return self.av["type"] in ("cd10", "mm97")
@@ -407,7 +420,9 @@ class Model:
             p.curlv = L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0)
         return p
 
-    def _config_struct(self):
+    def _config_struct(self, tier=None):
+        """The C configuration; tier: a concrete precision tier (GBSPH_FP64, GBSPH_MIXED or
+        GBSPH_MIXED_COMPENSATED) in place of the configured precision."""
         c = self.cfg
         if c.eos is None:
             raise RuntimeError("an equation of state must be set (set_eos_adiabatic or "
@@ -447,15 +462,18 @@ class Model:
         s.periodic = 1 if c.boundary == "periodic" else 0
         s.box_min = L.d3(self.box_min)
         s.box_max = L.d3(self.box_max)
-        s.precision = L.GBSPH_MIXED if c.precision == "mixed" else L.GBSPH_FP64
+        s.precision = PRECISION_CODES[c.precision] if tier is None else int(tier)
+        s.mixed_tol = getattr(c, "mixed_tol", 0.0)
         return s
 
     # ------------------------------------------------------------------ time stepping
-    def evolve_once(self, stream=None):
-        """Solver::evolve_once (Solver.cpp:1942-3272) on the GPU; returns the step log."""
+    def evolve_once(self, stream=None, tier=None):
+        """Solver::evolve_once (Solver.cpp:1942-3272) on the GPU; returns the step log.
+        tier: run this precision tier instead of the configured precision (a recompute of
+        an error-controlled step, given its log's "tier")."""
         lib = self._lib()
         p = self._particles_struct()
-        cfg = self._config_struct()
+        cfg = self._config_struct(tier)
         ts = L.TimeState(self.time, self.dt, self.cfl_mult)
         log = L.StepLog()
         import ctypes as C

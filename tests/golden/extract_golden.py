@@ -152,6 +152,8 @@ def extract_sedov(ref_root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python extract_golden.py <path of the Shamrock source checkout>")
+    root = sys.argv[1]
     extract(root)
     extract_sedov(root)
