@@ -364,8 +364,10 @@ def cpu_model():
     return platform.machine()
 
 
-def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
-    """FP64 oracle (OpenMP) on the same workload, bounded to about `seconds`."""
+def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0, first_step=None):
+    """FP64 oracle (OpenMP) on the same workload, bounded to about `seconds`.  first_step:
+    a dict that receives the set-up and the oracle's state after its first (untimed,
+    dt = 0) step, for the parity check against the GPU."""
     from oracle import oracle as O
 
     if threads:
@@ -374,7 +376,10 @@ def cpu_baseline(s, seconds, threads=None, alpha_AV=1.0):
     s, what = cpu_sample(s)
     oc = oracle_config(O, s, alpha_AV)
     sim = O.Sim(oc, s["pos"], s["vel"], s["h"], s["u"])
-    sim.evolve_once()  # dt = 0 step (h convergence, first CFL), untimed
+    log0 = sim.evolve_once()  # dt = 0 step (h convergence, first CFL), untimed
+    if first_step is not None:
+        first_step.update(setup=s, what=what, log=log0, state=sim.get(),
+                          av=sim.get_av() if s.get("av") == "cd10" else None)
     n = len(s["h"])
     t0 = time.time()
     steps = 0
@@ -488,6 +493,51 @@ def accuracy(s, alpha_AV=1.0, precision="mixed"):
                          "bit-identical to the FP64 oracle); rho per particle relative; a, du/dt, "
                          "omega normalised by the field's max magnitude (max) or rms (rms)")
     return res
+
+
+PARITY_FIELDS = ("xyz", "vxyz", "axyz", "hpart", "uint", "duint", "omega")
+PARITY_KEYS = ("n_ghost", "leaf_count", "cache_size", "h_subcycles", "h_iterations",
+               "corrector_iters", "next_dt", "cfl_mult")
+
+
+def oracle_parity(first, alpha_AV, precision):
+    """The GPU's first step against the oracle's from the same initial state (the set-up
+    the CPU leg timed: the full workload, or its 2^20-particle sample for the 33.8M
+    homogeneous box).  FP64: every field and the step's bookkeeping bit for bit.  Mixed:
+    max / RMS errors against the oracle (rho per particle, a, du/dt and Omega normalised
+    by the field's largest magnitude) and the precision tier the step ran in."""
+    import numpy as np
+
+    s, o = first["setup"], first["state"]
+    out = {"particles": int(len(s["h"])), "set_up": first["what"]}
+    m64 = make_model(s, "fp64", alpha_AV=alpha_AV)
+    l64 = m64.evolve_once()
+    g = m64.collect_data()
+    diff = [k for k in PARITY_FIELDS if not np.array_equal(g[k], o[k])]
+    if first.get("av") is not None:
+        diff += [k for k in ("alpha_AV", "soundspeed") if not np.array_equal(g[k], first["av"][k])]
+    diff += ["log." + k for k in PARITY_KEYS if l64[k] != first["log"][k]]
+    out["fp64_bitexact"] = not diff
+    out["fp64_mismatches"] = diff
+    del m64
+    mm = make_model(s, precision, alpha_AV=alpha_AV)
+    lm = mm.evolve_once()
+    d = mm.collect_data()
+    err = {}
+    rho_d, rho_o = s["pmass"] * (1.2 / d["hpart"]) ** 3, s["pmass"] * (1.2 / o["hpart"]) ** 3
+    rel = np.abs(rho_d - rho_o) / rho_o
+    err["rho"] = {"max": float(rel.max()), "rms": float(np.sqrt(np.mean(rel**2)))}
+    for k, key in (("axyz", "a"), ("duint", "du_dt"), ("omega", "omega")):
+        x, y = d[k], o[k]
+        if x.ndim > 1:
+            dx, ny = np.linalg.norm(x - y, axis=1), np.linalg.norm(y, axis=1)
+        else:
+            dx, ny = np.abs(x - y), np.abs(y)
+        err[key] = {"max": float(dx.max() / ny.max()),
+                    "rms": float(np.sqrt(np.mean(dx**2)) / np.sqrt(np.mean(ny**2)))}
+    err["tier"] = int(lm["tier"])
+    out["mixed_vs_oracle"] = err
+    return out
 
 
 def run_gb300(args):
@@ -609,8 +659,12 @@ def run_gb300(args):
         else:
             line["adjoint"] = adjoint_bench(precision=args.precision, device=local)
     if world == 1 and not args.no_cpu_baseline:
+        first = {}
         line["cpu_baseline"] = cpu_baseline(s, args.cpu_seconds, threads=os.cpu_count(),
-                                            alpha_AV=alpha_av)
+                                            alpha_AV=alpha_av, first_step=first)
+        if not args.no_accuracy:
+            prec = args.precision if args.precision.startswith("mixed") else "mixed"
+            line["parity_vs_oracle"] = oracle_parity(first, alpha_av, prec)
     print(json.dumps(line), flush=True)
     return 0
 

@@ -129,6 +129,11 @@ typedef struct {
      * (relative to the largest magnitude of each field) the FP32 tier may leave; 0 selects
      * 1e-5. */
     double mixed_tol;
+    /* Corrector evaluations after which a step that still fails the eps_v test gives up
+     * with GBSPH_ERR_NOT_CONVERGED (the reference stops at 50, Solver.cpp:2252-2256);
+     * 0 selects 50. */
+    uint32_t corrector_max_iters;
+    uint32_t pad3;
 } gbsph_config;
 
 #define GBSPH_EOS_ADIABATIC 0

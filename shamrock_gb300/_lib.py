@@ -52,7 +52,8 @@ class Config(C.Structure):
                 ("epsilon_h_particle", _f64), ("eos_kind", _u32), ("ext_kind", _u32),
                 ("cs0", _f64), ("eos_r0", _f64), ("eos_q", _f64), ("central_mass", _f64),
                 ("constant_G", _f64), ("av_kind", _u32), ("pad2", _u32), ("alpha_min", _f64),
-                ("alpha_max", _f64), ("sigma_decay", _f64), ("mixed_tol", _f64)]
+                ("alpha_max", _f64), ("sigma_decay", _f64), ("mixed_tol", _f64),
+                ("corrector_max_iters", _u32), ("pad3", _u32)]
 
 
 class TimeState(C.Structure):

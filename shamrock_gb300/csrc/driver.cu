@@ -772,7 +772,7 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
                           cfg->htol_up_coarse, cfg->htol_up_fine, c.omega_local.as<f64>()));
         CU(scatter_rows(c, n, c.hnew_row.as<f64>(), lf.h));
     } else if (mixed) {
-        CU(omega_mixed(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>()));
+        CU(omega_compact_mixed(c, rs, N, n, lf.h, c.hnew_row.as<f64>(), c.omega_local.as<f64>()));
     } else {
         CU(omega64(c, rs, c.hnew_row.as<f64>(), cfg->pmass, c.omega_local.as<f64>(),
                    c.row_local.as<u32>()));
@@ -797,11 +797,13 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     f64 next_cfl   = 0;
     bool rerun     = false;
     u32 corr_iters = 0;
+    const u32 corr_cap = cfg->corrector_max_iters ? cfg->corrector_max_iters : 50;
     do {
-        if (corr_iters == 50)
+        if (corr_iters == corr_cap)
             return fail(ctx, GBSPH_ERR_NOT_CONVERGED,
-                        "the corrector has made over 50 loops, either their is a bug, either you "
-                        "are using a dt that is too large");
+                        "the corrector has made over " + std::to_string(corr_cap) +
+                            " loops, either their is a bug, either you are using a dt that is "
+                            "too large");
         if (mixed)
             CU(gather_stage_mixed(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos, cd10, comp));
         else CU(gather_eos64(c, N, n, lf, c.omega_local.as<f64>(), cfg->pmass, eos));

@@ -277,6 +277,68 @@ __global__ void __launch_bounds__(256) k_omega_mixed(RowSpace rs, MixedSpace ms,
 }
 
 
+// 1/h lane of the position records from the converged smoothing lengths (the records
+// were staged with the h the neighbour cache was built with); the same value the
+// corrector staging writes, so the compaction below and the corrector kernels test
+// pairs alike.
+__global__ void k_restage_hinv(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
+                               const u32 *__restrict__ ghost_src, const f64 *__restrict__ h,
+                               float4 *__restrict__ P) {
+    u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    u32 id  = sort_index[r];
+    u32 src = id < n_local ? id : ghost_src[id - n_local];
+    ((float *) &P[2 * (size_t) r])[3] = __double2float_rn(rcp64(h[src]));
+}
+
+// Omega (as k_omega_mixed) and, in the same pass over the row, the row compacted in
+// place to the entries the corrector kernels can use: pairs inside either particle's
+// support at the converged h, the test of derivs_row_f32 (r^2 h_a^-2 > 4 and
+// r^2 h_b^-2 > 4 drops a pair), coincident pairs and the particle itself kept (the
+// density terms of the reverse pass include them).  About a quarter of a row lies
+// beyond both supports (the cache holds pairs within 1.1 h).  Writes trail reads
+// within the thread's own row, so the compaction is race-free.
+__global__ void __launch_bounds__(256) k_omega_compact_mixed(RowSpace rs, MixedSpace ms,
+                                                             const f64 *__restrict__ h_row,
+                                                             f64 *__restrict__ omega_local,
+                                                             u32 *ent_w, u32 *cnt_w) {
+    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rs.n) return;
+    const u32 a  = rs.row_rank[t];
+    const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+    const float hinv  = __double2float_rn(rcp64(h_row[t]));
+    const float hinv2 = hinv * hinv;
+    const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
+    float sg = 0.f, cg = 0.f;
+    u32 w = k0;
+    uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, true, a) : make_uint4(a, a, a, a);
+    for (u32 k = k0; k < k1; k += 4) {
+        const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
+        F8 pb[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) pb[j] = ldg256(&ms.P[2 * (size_t) bb[j]]);
+        if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, true, a);
+        float bg = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (k + j >= k1) continue;
+            float dx = (pa.a.x - pb[j].a.x) + (pa.b.x - pb[j].b.x);
+            float dy = (pa.a.y - pb[j].a.y) + (pa.b.y - pb[j].b.y);
+            float dz = (pa.a.z - pb[j].a.z) + (pa.b.z - pb[j].b.z);
+            float r2 = dx * dx + dy * dy + dz * dz;
+            const float hib = pb[j].a.w;
+            if (!(r2 * hinv2 > 4.f && r2 * (hib * hib) > 4.f)) ent_w[w++] = bb[j];
+            float q2 = r2 * hinv2;
+            if (q2 > 4.f) continue;
+            float q = sqrt_approx(q2);
+            bg += 3.f * m4_f32(q) + q * m4_df32(q);
+        }
+        kahan_add(sg, cg, bg);
+    }
+    cnt_w[t] = w - k0;
+    omega_local[rs.row_local[t]] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
+}
+
 // FP32 pair loop of the constant-AV derivatives; returns the bare sums
 //   F = sum (ca Fa + cb Fb) r_hat   (acceleration = -m F)
 //   U = sum [AVPa c1a Fa (v.r_hat) + 0.5 alpha_u vsig_u (u_a - u_b)(Fa c2a + Fb c2b)]
@@ -639,6 +701,20 @@ cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass,
     ProfScope ps(c, kProfOmega, rs.n);
     MixedSpace ms = mixed_space(c, c.n_obj);
     { k_omega_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(rs, ms, h_row, pmass, omega_local); GBSPH_COUNTED; }
+    return cudaGetLastError();
+}
+
+cudaError_t omega_compact_mixed(Ctx &c, const RowSpace &rs, u32 N, u32 n_local, const f64 *h_local,
+                                const f64 *h_row, f64 *omega_local) {
+    ProfScope ps(c, kProfOmega, rs.n);
+    MixedSpace ms = mixed_space(c, c.n_obj);
+    { k_restage_hinv<<<div_up(N, 256), 256, 0, c.stream>>>(c.sort_index.as<u32>(), N, n_local,
+                                                         c.ghost_src.as<u32>(), h_local,
+                                                         c.f_pos.as<float4>()); GBSPH_COUNTED; }
+    { k_omega_compact_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(
+        rs, ms, h_row, omega_local, c.csr_ent.as<u32>(), c.csr_cnt.as<u32>()); GBSPH_COUNTED; }
+    // the cache no longer holds the reference's pair set
+    c.cache_valid = false;
     return cudaGetLastError();
 }
 

@@ -28,6 +28,12 @@ cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h
                             f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters,
                             f64 eps_p = 1e-6);
 cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
+// the pipeline's Omega: restages the records' 1/h from the converged h (local ids), then
+// Omega per row and, in the same pass, each cache row compacted in place to the pairs
+// inside either support (the entries the corrector kernels visit); the cache is no
+// longer exportable afterwards (cache_valid = false)
+cudaError_t omega_compact_mixed(Ctx &c, const RowSpace &rs, u32 N, u32 n_local, const f64 *h_local,
+                                const f64 *h_row, f64 *omega_local);
 // the corrector's EOS + record staging for merged ranks 0..N-1 (replaces gather_eos64
 // + the FP64 rank-ordered copies in the mixed path; only h is kept in FP64, in c.sh2),
 // then the fused derivatives step, which reads the records, c.sh2 and the caller's

@@ -69,6 +69,9 @@ class SolverConfig:
         self.h_max_subcycles_count = 100
         self.precision = "fp64"
         self.mixed_tol = 0.0  # 0: the library's 1e-5
+        # corrector evaluations before a step gives up (the reference's fixed 50; GB300
+        # extension so that the give-up path can be exercised)
+        self.corrector_max_iters = 50
         self.ext_forces = []
         # G without a unit system is the SI value, as the reference's get_constant_G
         self.constant_G = G_SI
@@ -464,6 +467,7 @@ class Model:
         s.box_max = L.d3(self.box_max)
         s.precision = PRECISION_CODES[c.precision] if tier is None else int(tier)
         s.mixed_tol = getattr(c, "mixed_tol", 0.0)
+        s.corrector_max_iters = int(getattr(c, "corrector_max_iters", 50))
         return s
 
     # ------------------------------------------------------------------ time stepping
@@ -483,6 +487,14 @@ class Model:
         lib.check(rc)
         self.time, self.dt, self.cfl_mult = ts.t, ts.dt, ts.cfl_mult
         d = log.as_dict()
+        # a step that completed with a warning (the h iteration not converged after the
+        # last sub-cycle: the reference logs an error and carries on, Solver.cpp:1271-1273)
+        note = lib.lib.gbsph_last_error(lib.handle)
+        d["note"] = note.decode() if note else ""
+        if d["note"]:
+            import warnings
+
+            warnings.warn("evolve_once: " + d["note"], RuntimeWarning)
         self.logs.append(d)
         return d
 

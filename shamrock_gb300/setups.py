@@ -76,7 +76,7 @@ def _jittered_lattice(n_side, rng, jitter):
     return pos + (jitter / n_side) * rng.standard_normal(pos.shape)
 
 
-def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0, jitter=0.1):
+def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0, jitter=0.1, literal=False):
     """Half the particles uniform in the unit cube, half in a Gaussian clump of width sigma
     at the centre; v ~ N(0, 0.1^2) per component, u ~ U[0.5, 1.5].
 
@@ -88,10 +88,18 @@ def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0, jitter=0.1):
     density sum is dominated by close pairs, Omega < 0, and the h-rho Newton step of
     IterateSmoothingLengthDensity moves h away from the root every iteration (h then
     grows by the sub-cycle limit until it spans the box).  Lattice sampling keeps the
-    same density field without near-coincident pairs."""
+    same density field without near-coincident pairs.
+
+    literal: both halves as independent random points instead (uniform in the cube; the
+    clump N(0.5, sigma^2) per coordinate, clipped into the box), the configuration as
+    stated, which exercises the h iteration's non-convergence and restart path."""
     rng = np.random.default_rng(seed)
     n1 = N // 2
     n2 = N - n1
+    if literal:
+        p1 = rng.uniform(0.0, 1.0, size=(n1, 3))
+        p2 = np.clip(rng.normal(0.5, sigma, size=(n2, 3)), 1e-9, 1.0 - 1e-9)
+        return _clustered_fields(np.concatenate([p1, p2]), rng, N, sigma, gamma)
     # uniform half: smallest cubic lattice with >= n1 sites, random sites removed
     ns = int(np.ceil(n1 ** (1.0 / 3.0)))
     p1 = _jittered_lattice(ns, rng, jitter)
@@ -107,7 +115,10 @@ def clustered_box(N, seed=12345, sigma=0.05, gamma=5.0 / 3.0, jitter=0.1):
     r_new = sigma * np.interp(u_frac, P, rt)
     dirs = q / np.maximum(rq, 1e-300)[:, None]
     p2 = np.clip(0.5 + dirs * r_new[:, None], 1e-9, 1.0 - 1e-9)
-    pos = np.concatenate([p1, p2])
+    return _clustered_fields(np.concatenate([p1, p2]), rng, N, sigma, gamma)
+
+
+def _clustered_fields(pos, rng, N, sigma, gamma):
     vel = rng.normal(0.0, 0.1, size=(N, 3))
     u = rng.uniform(0.5, 1.5, size=N)
     pmass = 1.0 / N
