@@ -656,6 +656,9 @@ def run_gb300(args):
         if args.workload == "disc":
             line["adjoint"] = adjoint_bench(steps=50, ck=5, precision=args.precision, device=local,
                                             workload="disc")
+        elif args.workload == "homogeneous":
+            line["adjoint"] = adjoint_bench(steps=20, ck=5, precision=args.precision, device=local,
+                                            workload="homogeneous", n_target=args.n_target)
         else:
             line["adjoint"] = adjoint_bench(precision=args.precision, device=local)
     if world == 1 and not args.no_cpu_baseline:
@@ -669,7 +672,8 @@ def run_gb300(args):
     return 0
 
 
-def adjoint_bench(steps=40, ck=5, precision="mixed", device=0, workload="soundwave"):
+def adjoint_bench(steps=40, ck=5, precision="mixed", device=0, workload="soundwave",
+                  n_target=1 << 22):
     """Adjoint / forward time of a differentiable rollout of `steps` steps with a
     checkpoint every `ck` steps; gradients with respect to initial v, u and alpha_AV.
     soundwave: 2^18 particles (simple cubic 64^3), density perturbation 1e-4 sin(2 pi x),
@@ -685,10 +689,15 @@ def adjoint_bench(steps=40, ck=5, precision="mixed", device=0, workload="soundwa
     if workload == "disc":
         s = setups.keplerian_disc(4194304, seed=12345)
         alpha0 = 0.5
+    elif workload == "homogeneous":
+        # the reference's benchmark set-up with its varying (CD10) viscosity, advanced with
+        # the CFL step; differentiated parameters: the switch's alpha_min and alpha_max
+        s = dict(homogeneous_setup(n_target), dt_zero=False)
+        alpha0 = [0.0, 1.0]
     else:
         s = setups.sound_wave(n_side=64, amp=1e-4, gamma=1.0001)
         alpha0 = 0.1
-    m = make_model(s, precision, device, alpha_AV=alpha0)
+    m = make_model(s, precision, device, alpha_AV=0.0 if workload == "homogeneous" else alpha0)
     m.evolve_once()  # dt = 0: initial h, Omega, a, du
     d = m._to_device()
     n = d["hpart"].shape[0]
@@ -699,8 +708,9 @@ def adjoint_bench(steps=40, ck=5, precision="mixed", device=0, workload="soundwa
     alpha = torch.tensor(alpha0, dtype=torch.float64, requires_grad=True)
 
     def loss_of(v):
-        # disc: total kinetic energy; sound wave: distance to a seeded target field
-        if workload == "disc":
+        # disc, homogeneous box: total kinetic energy; sound wave: distance to a seeded
+        # target field
+        if workload in ("disc", "homogeneous"):
             return 0.5 * s["pmass"] * (v * v).sum()
         return ((v - v_t) ** 2).sum()
 
@@ -729,16 +739,22 @@ def adjoint_bench(steps=40, ck=5, precision="mixed", device=0, workload="soundwa
     lib.profile(False)
     f_ms, b_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
     iters = [r[2] for r in adjoint.rollout.last_records]
-    wname = ("keplerian_disc_4194304 (LP07, point mass, alpha_AV 0.5, free boundary); loss = "
-             "total kinetic energy" if workload == "disc" else
-             "sound_wave_cubic_64^3 (N=%d, amp 1e-4, gamma 1.0001, alpha_AV 0.1, periodic); loss "
-             "= |v - v_target|^2" % n)
+    if workload == "disc":
+        wname = ("keplerian_disc_4194304 (LP07, point mass, alpha_AV 0.5, free boundary); loss = "
+                 "total kinetic energy")
+    elif workload == "homogeneous":
+        wname = ("homogeneous_hcp_box_%d (the reference's benchmark set-up, varying CD10 viscosity "
+                 "alpha in [0, 1], CFL steps); loss = total kinetic energy; gradients with respect "
+                 "to v0, u0, alpha_min, alpha_max" % n)
+    else:
+        wname = ("sound_wave_cubic_64^3 (N=%d, amp 1e-4, gamma 1.0001, alpha_AV 0.1, periodic); "
+                 "loss = |v - v_target|^2" % n)
     return {"workload": wname,
             "precision": precision, "steps": steps, "checkpoint_every": ck,
             "forward_ms": f_ms, "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
             "loss": float(loss.detach()),
             "grad_norm": {"v": float(v0.grad.norm()), "u": float(u0.grad.norm()),
-                          "alpha": float(alpha.grad)},
+                          "alpha": alpha.grad.tolist()},
             "corrector_iters": iters,
             "backward_stages_ms": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
             "definition": "backward (recompute between checkpoints + reverse steps) / forward "

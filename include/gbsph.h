@@ -363,6 +363,12 @@ typedef struct {
     uint32_t pad;
     gbsph_vec3 gx, gv, ga; /* positions, velocities, accelerations */
     double *gu, *gdu;      /* internal energy and its rate */
+    /* Varying viscosity (GBSPH_AV_VARYING_CD10 / _MM97) only, NULL otherwise: the
+     * per-particle alpha_AV and stored sound speed (device arrays, n each, in/out like
+     * the others), and host accumulators incremented by dL/d alpha_min, alpha_max and
+     * sigma_decay of the step's switch. */
+    double *galpha, *gsoundspeed;
+    double g_alpha_min, g_alpha_max, g_sigma_decay;
 } gbsph_cotangents;
 
 /* Reverse mode of one evolve_once (no reference counterpart: the differentiable step
@@ -373,8 +379,13 @@ typedef struct {
  * reversed: on entry `cot` holds dL/d(state after the step), on return dL/d(state
  * before it).  h after the step is treated as the exact solution of the density
  * constraint; dt and the neighbour set are held fixed.  *g_alpha_av (host) is
- * incremented by dL/d alpha_AV of this step.  FP64 reverse pass; the recompute runs in
- * cfg->precision. */
+ * incremented by dL/d alpha_AV of this step (constant viscosity).  With a varying
+ * viscosity `start` also gives alpha_AV and soundspeed, the velocity gradients and the
+ * switch are reversed too, and cot->galpha / gsoundspeed / g_alpha_min / g_alpha_max /
+ * g_sigma_decay carry their cotangents.  The recompute runs in cfg->precision (a
+ * concrete tier: GBSPH_FP64, GBSPH_MIXED or GBSPH_MIXED_COMPENSATED, the tier the
+ * forward step ran in); the reverse pass is FP64 after an FP64 recompute and FP32 pair
+ * arithmetic with FP64 accumulators after a mixed one. */
 int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
                        double t, double dt, uint32_t corrector_iters, gbsph_cotangents *cot,
                        double *g_alpha_av, void *stream);

@@ -73,7 +73,8 @@ class StepLog(C.Structure):
 
 class Cotangents(C.Structure):
     _fields_ = [("n", _u32), ("pad", _u32), ("gx", Vec3), ("gv", Vec3), ("ga", Vec3),
-                ("gu", _vp), ("gdu", _vp)]
+                ("gu", _vp), ("gdu", _vp), ("galpha", _vp), ("gsoundspeed", _vp),
+                ("g_alpha_min", _f64), ("g_alpha_max", _f64), ("g_sigma_decay", _f64)]
 
 
 _P = C.POINTER

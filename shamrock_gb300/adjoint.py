@@ -5,9 +5,13 @@ The reference has no adjoint; this is the differentiable form of its step
 
 ``rollout(model, v0, u0, alpha, n_steps, checkpoint_every, dts=None)`` runs ``n_steps``
 steps of ``model`` from its current positions, h, a and du with initial velocities
-``v0`` (3, N), internal energies ``u0`` (N,) and constant-AV ``alpha`` (alpha_AV), and
+``v0`` (3, N), internal energies ``u0`` (N,) and the viscosity parameters ``alpha``, and
 returns the final ``(x, v, u)``.  Gradients flow to ``v0``, ``u0``, ``alpha`` and the
-initial positions ``x0`` when given.
+initial positions ``x0`` when given.  ``alpha`` is alpha_AV (a scalar) for the constant
+viscosity, and (alpha_min, alpha_max) for the varying ones (Cullen & Dehnen 2010, Morris &
+Monaghan 1997), whose per-particle alpha_AV and stored sound speed are then part of the
+state each step carries (their gradients, and that of sigma_decay, are kept in
+``rollout.last_av_grads``).
 
 What is differentiated: the step map with each step's dt, its number of corrector
 evaluations and its neighbour cache held at the forward pass's values; h after each
@@ -25,16 +29,25 @@ import ctypes as C
 from . import _lib as L
 
 STATE_KEYS = ("xyz", "vxyz", "axyz", "hpart", "uint", "duint")
+AV_STATE_KEYS = ("alpha_AV", "soundspeed")
+
+
+def _varying(model):
+    return model.cfg.av["type"] in ("cd10", "mm97")
+
+
+def _keys(model):
+    return STATE_KEYS + (AV_STATE_KEYS if _varying(model) else ())
 
 
 def _snapshot(model):
     d = model._to_device()
-    return {k: d[k].clone() for k in STATE_KEYS}
+    return {k: d[k].clone() for k in _keys(model)}
 
 
 def _restore(model, snap):
     d = model._to_device()
-    for k in STATE_KEYS:
+    for k in _keys(model):
         d[k].copy_(snap[k])
 
 
@@ -48,6 +61,9 @@ def _particles_of(snap):
     p.uint = snap["uint"].data_ptr()
     p.duint = snap["duint"].data_ptr()
     p.omega = None
+    if "alpha_AV" in snap:
+        p.alpha_AV = snap["alpha_AV"].data_ptr()
+        p.soundspeed = snap["soundspeed"].data_ptr()
     return p
 
 
@@ -59,6 +75,9 @@ def _cot_struct(cot):
         setattr(c, name, L.Vec3(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 1, 0))
     c.gu = cot["gu"].data_ptr()
     c.gdu = cot["gdu"].data_ptr()
+    if "galpha" in cot:
+        c.galpha = cot["galpha"].data_ptr()
+        c.gsoundspeed = cot["gcs"].data_ptr()
     return c
 
 
@@ -78,6 +97,10 @@ def adjoint_step(model, start, t, dt, corrector_iters, cot, tier=None):
     lib.check(lib.lib.gbsph_adjoint_step(lib.handle, C.byref(p), C.byref(cfg), float(t),
                                          float(dt), int(corrector_iters), C.byref(cs),
                                          C.byref(g_alpha), None))
+    if "g_av" in cot:
+        cot["g_av"][0] += cs.g_alpha_min
+        cot["g_av"][1] += cs.g_alpha_max
+        cot["g_av"][2] += cs.g_sigma_decay
     return g_alpha.value
 
 
@@ -141,11 +164,14 @@ class _Rollout:
         return g_alpha
 
 
-def _zero_cot(n, dev):
+def _zero_cot(n, dev, varying=False):
     import torch
 
     z = lambda *s: torch.zeros(*s, dtype=torch.float64, device=dev)
-    return dict(gx=z(3, n), gv=z(3, n), ga=z(3, n), gu=z(n), gdu=z(n))
+    cot = dict(gx=z(3, n), gv=z(3, n), ga=z(3, n), gu=z(n), gdu=z(n))
+    if varying:
+        cot.update(galpha=z(n), gcs=z(n), g_av=[0.0, 0.0, 0.0])
+    return cot
 
 
 def rollout(model, v0, u0, alpha, n_steps, checkpoint_every=5, dts=None, x0=None):
@@ -161,7 +187,11 @@ def rollout(model, v0, u0, alpha, n_steps, checkpoint_every=5, dts=None, x0=None
                 d["xyz"].copy_(x0_)
             d["vxyz"].copy_(v0_)
             d["uint"].copy_(u0_)
-            model.cfg.av["alpha_AV"] = float(alpha_)
+            if _varying(model):
+                model.cfg.av["alpha_min"] = float(alpha_[0])
+                model.cfg.av["alpha_max"] = float(alpha_[1])
+            else:
+                model.cfg.av["alpha_AV"] = float(alpha_)
             ro = _Rollout(model, n_steps, checkpoint_every, dts)
             ro.forward()
             ctx.ro = ro
@@ -175,7 +205,8 @@ def rollout(model, v0, u0, alpha, n_steps, checkpoint_every=5, dts=None, x0=None
         def backward(ctx, gx, gv, gu):
             n = gu.shape[0] if gu is not None else model.get_total_part_count()
             dev = model._to_device()["hpart"].device
-            cot = _zero_cot(n, dev)
+            var = _varying(model)
+            cot = _zero_cot(n, dev, var)
             if gx is not None:
                 cot["gx"].copy_(gx)
             if gv is not None:
@@ -183,12 +214,18 @@ def rollout(model, v0, u0, alpha, n_steps, checkpoint_every=5, dts=None, x0=None
             if gu is not None:
                 cot["gu"].copy_(gu)
             g_alpha = ctx.ro.backward(cot)
-            ga = torch.tensor(g_alpha, dtype=torch.float64)
+            if var:
+                ga = torch.tensor(cot["g_av"][:2], dtype=torch.float64)
+                rollout.last_av_grads = dict(alpha_AV=cot["galpha"], soundspeed=cot["gcs"],
+                                             sigma_decay=cot["g_av"][2])
+            else:
+                ga = torch.tensor(g_alpha, dtype=torch.float64)
             return cot["gv"], cot["gu"], ga, (cot["gx"] if ctx.has_x0 else None)
 
-    alpha_t = alpha if isinstance(alpha, torch.Tensor) else torch.tensor(float(alpha), dtype=torch.float64)
+    alpha_t = alpha if isinstance(alpha, torch.Tensor) else torch.tensor(alpha, dtype=torch.float64)
     return Fn.apply(v0, u0, alpha_t, x0)
 
 
 rollout.last_dts = None
 rollout.last_records = None
+rollout.last_av_grads = None

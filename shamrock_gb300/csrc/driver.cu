@@ -64,7 +64,7 @@ Ctx::~Ctx() {
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
                       &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2, &f_comp, &guard_state,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
-                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &aext, &av_arank,
+                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &adj_snap_av, &adj_vg, &aext, &av_arank,
                       &av_alpha_rank, &av_alpha_upd, &av_diag};
     cudaSetDevice(device);
     for (DevBuf *b : bufs) b->release(stream);
@@ -606,22 +606,23 @@ int gbsph_ghost_export(gbsph_ctx *ctx, uint32_t *src, uint8_t *offset_id, double
 
 } // extern "C"
 
-// Estimated relative error of the FP32 tier's accelerations and du/dt on the last
-// corrector evaluation: the FP32 rounding of the pair terms, and of the h, rho, P, Omega
-// and u they are built from, errs in proportion to the summed term magnitudes, which the
-// derivatives pass accumulates per row; divided by the largest result.  The effective
-// relative error per unit of condition is 3e-7 for both: measured 1.4e-7 for the forces
-// on the 64^3 sound wave (condition 3.2e4, error 4.4e-3), 6e-8 for du/dt there
-// (condition 4.4e3, error 2.6e-4) and 1.8e-7 for du/dt on a Sedov blast (condition 1.3,
-// error 2.4e-7: the rounding of well-conditioned FP32 sums).  A field that vanishes
-// while its terms do not is taken as unbounded error.
-static constexpr f64 kErrEffA  = 3e-7;
-static constexpr f64 kErrEffDu = 3e-7;
-static f64 err_estimate(f64 eff, u64 sum_bits, u64 max_bits) {
+// Estimated relative error of the FP32 tier's accelerations and du/dt on the first
+// corrector evaluation of a step: the FP32 rounding of the pair terms, and of the h, rho,
+// P, Omega and u they are built from, errs in proportion to the summed term magnitudes,
+// which the derivatives pass accumulates per row.  With the condition C = largest sum /
+// largest result of a field, the estimate is 3e-7 + 1.5e-7 C: measured errors per unit
+// of condition (one step, FP32 tier against FP64) span 1.5e-8 to 1.4e-7 on the Sedov,
+// clustered, sound-wave, disc and homogeneous workloads (C from 1 to 3.2e4), and
+// 2.4e-7 at C = 1 (the rounding of well-conditioned sums); the estimate is above every
+// measured error.  A field that vanishes while its terms do not is taken as unbounded
+// error.
+static constexpr f64 kErrBase = 3e-7;
+static constexpr f64 kErrCond = 1.5e-7;
+static f64 err_estimate(u64 sum_bits, u64 max_bits) {
     const f64 s = ordered_to_f64(sum_bits), m = ordered_to_f64(max_bits);
     if (!(s > 0)) return 0;
     if (!(m > 0)) return std::numeric_limits<f64>::infinity();
-    return eff * s / m;
+    return kErrBase + kErrCond * s / m;
 }
 
 // One step (Solver::evolve_once) in one precision tier (GBSPH_FP64, GBSPH_MIXED or
@@ -651,7 +652,6 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     const bool cd10 = cfg->av_kind != GBSPH_AV_CONSTANT;
     REQUIRE_ARG(!cd10 || (p->alpha_AV && p->soundspeed),
                 "the varying viscosity needs the alpha_AV and soundspeed fields");
-    REQUIRE_ARG(!cd10 || !tape, "the adjoint step supports the constant viscosity only");
     REQUIRE_ARG(!cd10 || !p->curlv.x || (p->curlv.y && p->curlv.z && p->curlv.stride > 0),
                 "curlv needs its three components and a stride");
     auto t_start = std::chrono::steady_clock::now();
@@ -790,6 +790,7 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     }
     if (tape) {
         CU(tape->snap->ensure(sizeof(f64) * 4 * (size_t) n * tape->forced_iters, s));
+        if (cd10) CU(tape->snap_av->ensure(sizeof(f64) * 4 * (size_t) n * tape->forced_iters, s));
         tape->iters = 0;
     }
     HydroSpace hs{c.sh2.as<f64>(), c.su.as<f64>(),  c.svx.as<f64>(), c.svy.as<f64>(),
@@ -857,6 +858,13 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             { k_snap_vu<<<div_up(n, 256), 256, 0, s>>>(
                 n, lf.vx, lf.vy, lf.vz, lf.vs, lf.u,
                 tape->snap->as<f64>() + (size_t) corr_iters * 4 * n); GBSPH_COUNTED; }
+            if (cd10) {
+                // the velocity gradients' accelerations (the previous evaluation's) and this
+                // evaluation's switched alpha
+                { k_snap_vu<<<div_up(n, 256), 256, 0, s>>>(
+                    n, lf.ax, lf.ay, lf.az, lf.vs, c.av_alpha_upd.as<f64>(),
+                    tape->snap_av->as<f64>() + (size_t) corr_iters * 4 * n); GBSPH_COUNTED; }
+            }
             tape->iters = corr_iters + 1;
         }
         { k_reset_corrector<<<1, 1, 0, s>>>(dsc); GBSPH_COUNTED; }
@@ -915,8 +923,8 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     lg.rate            = elapsed > 0 ? f64(n) / elapsed : 0;
     lg.tier            = tier;
     if (mixed) {
-        lg.err_est_a  = err_estimate(kErrEffA, c.h_scalars->cond_fa, c.h_scalars->cond_a);
-        lg.err_est_du = err_estimate(kErrEffDu, c.h_scalars->cond_fu, c.h_scalars->cond_du);
+        lg.err_est_a  = err_estimate(c.h_scalars->cond_fa, c.h_scalars->cond_a);
+        lg.err_est_du = err_estimate(c.h_scalars->cond_fu, c.h_scalars->cond_du);
     }
     if (log) *log = lg;
     if (!converged) ctx->c.err = "the h iterator is not converged after the maximum number of "
@@ -1030,15 +1038,25 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
                     !cfg->periodic,
                 "the adjoint of the locally isothermal EOS or the point mass needs free "
                 "boundaries (a periodic image's pressure depends on its shifted position)");
+    const bool var = cfg->av_kind != GBSPH_AV_CONSTANT;
+    REQUIRE_ARG(!var || (start->alpha_AV && start->soundspeed && cot->galpha && cot->gsoundspeed),
+                "the varying viscosity's adjoint needs alpha_AV and soundspeed in the start state "
+                "and galpha and gsoundspeed in the cotangents");
+    REQUIRE_ARG(cfg->precision != GBSPH_MIXED_GUARDED,
+                "give the adjoint step the tier the forward step ran in (gbsph_step_log.tier)");
     cudaStream_t s = c.stream;
     const u32 n    = start->n;
     // recompute the step on a working copy of the start state
-    CU(c.adj_state.ensure(sizeof(f64) * 12 * (size_t) n, s));
+    CU(c.adj_state.ensure(sizeof(f64) * 14 * (size_t) n, s));
     f64 *W = c.adj_state.as<f64>();
     size_t n_ = n;
     { k_copy_state<<<div_up(n, 256), 256, 0, s>>>(n, start->xyz, start->vxyz, start->axyz,
                                                 start->hpart, start->uint, start->duint, W); GBSPH_COUNTED; }
     CU(cudaGetLastError());
+    if (var) {
+        CU(cudaMemcpyAsync(W + 12 * n_, start->alpha_AV, 8 * n_, cudaMemcpyDeviceToDevice, s));
+        CU(cudaMemcpyAsync(W + 13 * n_, start->soundspeed, 8 * n_, cudaMemcpyDeviceToDevice, s));
+    }
     gbsph_particles w;
     std::memset(&w, 0, sizeof(w));
     w.n     = n;
@@ -1048,10 +1066,15 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     w.hpart = W + 9 * n_;
     w.uint  = W + 10 * n_;
     w.duint = W + 11 * n_;
+    if (var) {
+        w.alpha_AV   = W + 12 * n_;
+        w.soundspeed = W + 13 * n_;
+    }
     gbsph_time_state ts{t, dt, 1.0};
     StepTape tape;
     tape.forced_iters = corrector_iters;
     tape.snap         = &c.adj_snap;
+    tape.snap_av      = &c.adj_snap_av;
     int st = evolve_impl(ctx, &w, cfg, &ts, nullptr, &tape);
     if (st != GBSPH_OK) return st;
     RowSpace rs{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
@@ -1059,7 +1082,10 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
                 c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
     AdjParams ap{cfg->pmass, cfg->gamma, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV, dt,
                  cfg->eos_kind, cfg->cs0, cfg->eos_r0 > 0 ? cfg->eos_r0 : 1.0, cfg->eos_q,
-                 -cfg->central_mass * cfg->constant_G, nullptr, nullptr, nullptr};
+                 -cfg->central_mass * cfg->constant_G, nullptr, nullptr, nullptr,
+                 cfg->av_kind, cfg->alpha_min, cfg->alpha_max, cfg->sigma_decay,
+                 var ? start->alpha_AV : nullptr, var ? start->soundspeed : nullptr,
+                 w.xyz.x, w.xyz.y, w.xyz.z};
     if (cfg->ext_kind == GBSPH_EXT_POINT_MASS) {
         ap.ext_x = w.xyz.x;
         ap.ext_y = w.xyz.y;
@@ -1072,13 +1098,21 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     cs.u    = cot->gu;
     cs.du   = cot->gdu;
     cs.vs   = cot->gx.stride;
+    cs.alpha = var ? cot->galpha : nullptr;
+    cs.cs    = var ? cot->gsoundspeed : nullptr;
     Scalars *dsc = c.d_scalars.as<Scalars>();
     CU(cudaMemsetAsync(&dsc->g_alpha, 0, sizeof(f64), s));
+    CU(cudaMemsetAsync(dsc->g_av, 0, 3 * sizeof(f64), s));
     // FP32 reverse pass after either mixed tier's recompute, FP64 after the FP64 one
     CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), tape, ap, cs, &dsc->g_alpha,
-                        cfg->precision != GBSPH_FP64));
+                        dsc->g_av, cfg->precision != GBSPH_FP64));
     CU(sync_scalars(c));
     if (g_alpha_av) *g_alpha_av += c.h_scalars->g_alpha;
+    if (var) {
+        cot->g_alpha_min += c.h_scalars->g_av[0];
+        cot->g_alpha_max += c.h_scalars->g_av[1];
+        cot->g_sigma_decay += c.h_scalars->g_av[2];
+    }
     return GBSPH_OK;
 }
 

@@ -35,6 +35,7 @@ struct Scalars {
     u64 cond_du;       // ordered-u64 max |bare du/dt sum|
     f64 sum_v2;        // sum of |v|^2 after the corrector
     f64 g_alpha;       // adjoint: dL / d alpha_AV of one step
+    f64 g_av[3];       // adjoint: dL / d (alpha_min, alpha_max, sigma_decay) of one step
     f64 cons[8];       // conservation totals (momentum, energies)
     u32 total;         // scan totals
     u32 total2;
@@ -163,7 +164,7 @@ struct Ctx {
     DevBuf dt_part;
 
     // ---- adjoint: working state, tape, accumulators (local and rank order)
-    DevBuf adj_state, adj_snap, adj_loc, adj_rank;
+    DevBuf adj_state, adj_snap, adj_loc, adj_rank, adj_snap_av, adj_vg;
 
     ~Ctx();
 };

@@ -297,7 +297,8 @@ __global__ void k_restage_hinv(const u32 *__restrict__ sort_index, u32 N, u32 n_
 // r^2 h_b^-2 > 4 drops a pair), coincident pairs and the particle itself kept (the
 // density terms of the reverse pass include them).  About a quarter of a row lies
 // beyond both supports (the cache holds pairs within 1.1 h).  Writes trail reads
-// within the thread's own row, so the compaction is race-free.
+// within the thread's own row (a group of four is written only after its four entries
+// and the next four have been read), so the compaction is race-free.
 __global__ void __launch_bounds__(256) k_omega_compact_mixed(RowSpace rs, MixedSpace ms,
                                                              const f64 *__restrict__ h_row,
                                                              f64 *__restrict__ omega_local,
@@ -310,7 +311,10 @@ __global__ void __launch_bounds__(256) k_omega_compact_mixed(RowSpace rs, MixedS
     const float hinv2 = hinv * hinv;
     const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
     float sg = 0.f, cg = 0.f;
-    u32 w = k0;
+    // kept entries are collected four at a time and written with one 128-bit store
+    // (rows start on 16-byte boundaries and their slots are padded to four entries)
+    u32 w = k0, p = 0;
+    uint4 pend = make_uint4(a, a, a, a);
     uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, true, a) : make_uint4(a, a, a, a);
     for (u32 k = k0; k < k1; k += 4) {
         const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
@@ -327,7 +331,18 @@ __global__ void __launch_bounds__(256) k_omega_compact_mixed(RowSpace rs, MixedS
             float dz = (pa.a.z - pb[j].a.z) + (pa.b.z - pb[j].b.z);
             float r2 = dx * dx + dy * dy + dz * dz;
             const float hib = pb[j].a.w;
-            if (!(r2 * hinv2 > 4.f && r2 * (hib * hib) > 4.f)) ent_w[w++] = bb[j];
+            if (!(r2 * hinv2 > 4.f && r2 * (hib * hib) > 4.f)) {
+                const u32 b = bb[j];
+                pend.x = p == 0 ? b : pend.x;
+                pend.y = p == 1 ? b : pend.y;
+                pend.z = p == 2 ? b : pend.z;
+                pend.w = p == 3 ? b : pend.w;
+                if (++p == 4) {
+                    *(uint4 *) (ent_w + w) = pend;
+                    w += 4;
+                    p = 0;
+                }
+            }
             float q2 = r2 * hinv2;
             if (q2 > 4.f) continue;
             float q = sqrt_approx(q2);
@@ -335,7 +350,8 @@ __global__ void __launch_bounds__(256) k_omega_compact_mixed(RowSpace rs, MixedS
         }
         kahan_add(sg, cg, bg);
     }
-    cnt_w[t] = w - k0;
+    if (p) *(uint4 *) (ent_w + w) = pend; // the tail (slots past it hold stale entries)
+    cnt_w[t] = w - k0 + p;
     omega_local[rs.row_local[t]] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
 }
 
