@@ -511,12 +511,17 @@ __global__ void __launch_bounds__(256) k_adj_omega_b(RowSpace rs, Src src, f64 p
 // then the switch gives alpha of the evaluation from (div v, curl v, d(div v)/dt) and the
 // step's input alpha_AV, sound speed and h (UpdateViscosity.cpp:53-118, 122-215).
 // Reverse: pass A recomputes a row's sums, reverses the switch with the row's alpha
-// cotangent (from the derivatives' reverse), and writes the cotangents of the sums as 31
-// numbers per particle:
-//   Rb (3x3, Rb[i][j] at 3i + j), Dvb (Dvb[j][i] at 9 + 3j + i), Dab (18 + 3j + i), sdb, scb;
-// pass B gathers, for row c, the derivative with respect to c's position, velocity and
-// previous acceleration of every pair term c enters: its own row's (with its own
-// cotangents) and each neighbour's (with the neighbour's, staged by rank).
+// cotangent (from the derivatives' reverse), and folds the cotangents of the sums into 24
+// numbers per particle: with Rb, Dvb, Dab, sdb, scb the cotangents of R, Dv, Da, sd, sc,
+// a pair's linearised contribution is, for g = m F e,
+//   d/dv = Qv g,  d/dw = Qw g,  d/dr = -Rs g + (terms through g(r)),
+//   d/dg = Qv^T v - Rs r + Qw^T w,
+// with Qv = sdb I - Dvb^T + C(scb) (C(s) g = g x s), Qw = -Dab^T and Rs the symmetric part
+// of Rb (R's terms r_i g_j are symmetric, so only Rs enters): Rs (6, xx xy xz yy yz zz),
+// Qv (9, row-major), Qw (9).  Pass B gathers, for row c, the derivative with respect to
+// c's position, velocity and previous acceleration of every pair term c enters: its own
+// row's (with its own cotangents) and each neighbour's (with the neighbour's, staged by
+// rank: 96 bytes, three 256-bit loads in FP32).
 
 // velocity-gradient sources: per rank position, v of the evaluation, A of the previous
 // one, h and the staged cotangents of the sums
@@ -542,14 +547,14 @@ struct VG64 {
         dw[2] = r.az - az[b];
         hb    = h[b];
     }
-    __device__ void mat(u32 b, f64 out[31]) const {
+    __device__ void mat(u32 b, f64 out[24]) const {
         const f64 *q = M + 32 * (size_t) b;
 #pragma unroll
-        for (int k = 0; k < 31; k++) out[k] = q[k];
+        for (int k = 0; k < 24; k++) out[k] = q[k];
     }
 };
 // FP32: the position and velocity records of the derivatives' reverse (hi/lo pairs),
-// A[r] = {A_x, A_y, A_z, alpha}, M: 8 float4 per rank
+// A[r] = {A_x, A_y, A_z, alpha}, M: 6 float4 per rank (24 floats, 32-byte aligned)
 struct VG32 {
     using T = float;
     const float4 *P, *V, *A, *M;
@@ -576,50 +581,46 @@ struct VG32 {
         dw[2] = r.a.z - a.z;
         hb    = p.a.w;
     }
-    __device__ void mat(u32 b, float out[31]) const {
-        const float4 *q = M + 8 * (size_t) b;
+    __device__ void mat(u32 b, float out[24]) const {
+        const float4 *q = M + 6 * (size_t) b;
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const float4 v = __ldg(&q[k]);
-            out[4 * k] = v.x;
-            if (4 * k + 1 < 31) out[4 * k + 1] = v.y;
-            if (4 * k + 2 < 31) out[4 * k + 2] = v.z;
-            if (4 * k + 3 < 31) out[4 * k + 3] = v.w;
+        for (int k = 0; k < 3; k++) {
+            const F8 v = ldg256(&q[2 * k]);
+            out[8 * k + 0] = v.a.x;
+            out[8 * k + 1] = v.a.y;
+            out[8 * k + 2] = v.a.z;
+            out[8 * k + 3] = v.a.w;
+            out[8 * k + 4] = v.b.x;
+            out[8 * k + 5] = v.b.y;
+            out[8 * k + 6] = v.b.z;
+            out[8 * k + 7] = v.b.w;
         }
     }
 };
 
-// d/d(r, v, w) of one pair term sum_ij(...) of a row with cotangents M, given
+// d/d(r, v, w) of one pair term of a row with folded cotangents M (Rs, Qv, Qw), given
 // g = m F e: dr (direct and through g), dv, dw, and ge = (dL/dg).e for the h derivative
 template<class T>
-__device__ __forceinline__ void vg_pair_grad(const T M[31], T m, T F, T Fr, T rr, const T e[3],
+__device__ __forceinline__ void vg_pair_grad(const T M[24], T m, T F, T Fr, T rr, const T e[3],
                                              const T r[3], const T v[3], const T w[3], T dr[3],
                                              T dv[3], T dw[3], T &ge) {
     const T g[3] = {m * F * e[0], m * F * e[1], m * F * e[2]};
-    const T sd = M[27], s[3] = {M[28], M[29], M[30]};
-    const T gxs[3] = {g[1] * s[2] - g[2] * s[1], g[2] * s[0] - g[0] * s[2], g[0] * s[1] - g[1] * s[0]};
-    const T sxv[3] = {s[1] * v[2] - s[2] * v[1], s[2] * v[0] - s[0] * v[2], s[0] * v[1] - s[1] * v[0]};
+    const T Rs[3][3] = {{M[0], M[1], M[2]}, {M[1], M[3], M[4]}, {M[2], M[4], M[5]}};
     T gb[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        T a = sd * g[i] + gxs[i], b = T(0), c = T(0);
+        T a = 0, b = 0, c = 0, d = 0;
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            a -= M[9 + 3 * j + i] * g[j];
-            b -= M[18 + 3 * j + i] * g[j];
-            c -= M[3 * i + j] * g[j];
+            a += M[6 + 3 * i + j] * g[j];
+            b += M[15 + 3 * i + j] * g[j];
+            c -= Rs[i][j] * g[j];
+            d += M[6 + 3 * j + i] * v[j] - Rs[i][j] * r[j] + M[15 + 3 * j + i] * w[j];
         }
         dv[i] = a;
         dw[i] = b;
         dr[i] = c;
-    }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        T a = sd * v[j] + sxv[j];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-            a -= M[3 * i + j] * r[i] + M[9 + 3 * j + i] * v[i] + M[18 + 3 * j + i] * w[i];
-        gb[j] = a;
+        gb[i] = d;
     }
     ge = gb[0] * e[0] + gb[1] * e[1] + gb[2] * e[2];
     const T ir = T(1) / rr;
@@ -726,17 +727,41 @@ template<class VS>
 __global__ void __launch_bounds__(128) k_adj_vg_a(RowSpace rs, VS src, AdjParams p, AdjLocal L,
                                                   const f64 *__restrict__ h_local,
                                                   const f64 *__restrict__ om_local,
-                                                  f64 *__restrict__ Mloc, f64 *g_av) {
+                                                  f64 *__restrict__ Mloc, f64 *g_av,
+                                                  const float *__restrict__ taped) {
     using T = typename VS::T;
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     f64 gpar[3] = {0, 0, 0};
     if (t < rs.n) {
         const u32 c = rs.row_rank[t], i = rs.row_local[t];
-        const auto rc = src.row(c);
-        const T hc = src.hrow(rc), m = T(p.pmass), sig = T(kNorm3d);
-        const T ihc = T(1) / hc, ih4 = ihc * ihc * ihc * ihc;
+        const T m = T(p.pmass), sig = T(kNorm3d);
         T R[3][3] = {}, Dv[3][3] = {}, Da[3][3] = {}, sd = 0, sc[3] = {0, 0, 0};
-        const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+        const u32 k0 = rs.off[t], k1 = taped ? k0 : k0 + rs.cnt[t];
+        if (taped) {
+            // the forward pass's own sums (bare, times the pair mass here)
+            const float *q = taped + 24 * (size_t) i;
+            R[0][0] = m * T(q[0]);
+            R[0][1] = R[1][0] = m * T(q[1]);
+            R[0][2] = R[2][0] = m * T(q[2]);
+            R[1][1] = m * T(q[3]);
+            R[1][2] = R[2][1] = m * T(q[4]);
+            R[2][2] = m * T(q[5]);
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    Dv[a][b] = m * T(q[6 + 3 * a + b]);
+                    Da[a][b] = m * T(q[15 + 3 * a + b]);
+                }
+            // sd = sum v.g = -tr Dv, sc = sum v x g: sc_x = Dv[1][2] - Dv[2][1], ...
+            sd    = -(Dv[0][0] + Dv[1][1] + Dv[2][2]);
+            sc[0] = Dv[1][2] - Dv[2][1];
+            sc[1] = Dv[2][0] - Dv[0][2];
+            sc[2] = Dv[0][1] - Dv[1][0];
+        }
+        const auto rc = src.row(c);
+        const T hc = src.hrow(rc);
+        const T ihc = T(1) / hc, ih4 = ihc * ihc * ihc * ihc;
         for (u32 k = k0; k < k1; k++) {
             T d[3], dv[3], dw[3], hb;
             src.pair(rs.ent[k], rc, d, dv, dw, hb);
@@ -802,8 +827,8 @@ __global__ void __launch_bounds__(128) k_adj_vg_a(RowSpace rs, VS src, AdjParams
         for (int a = 0; a < 3; a++)
 #pragma unroll
             for (int b = 0; b < 3; b++) Gvb[a][b] = T(-2) * gt * Gv[b][a];
-        f64 *out = Mloc + 32 * (size_t) i;
         // Dab[q][b] = sum_a Ri[a][q] Gab[a][b] = gt Ri[b][q]; Dvb[q][b] = sum_a Ri[a][q] Gvb[a][b]
+        T Dvb[3][3], Dab[3][3];
 #pragma unroll
         for (int q = 0; q < 3; q++)
 #pragma unroll
@@ -811,8 +836,8 @@ __global__ void __launch_bounds__(128) k_adj_vg_a(RowSpace rs, VS src, AdjParams
                 T dvb = 0;
 #pragma unroll
                 for (int a = 0; a < 3; a++) dvb += Ri[a][q] * Gvb[a][b];
-                out[9 + 3 * q + b]  = (f64) dvb;
-                out[18 + 3 * q + b] = (f64) (gt * Ri[b][q]);
+                Dvb[q][b] = dvb;
+                Dab[q][b] = gt * Ri[b][q];
             }
         // Rib[a][q] = sum_b Gab[a][b] Da[q][b] + Gvb[a][b] Dv[q][b]
 #pragma unroll
@@ -825,6 +850,7 @@ __global__ void __launch_bounds__(128) k_adj_vg_a(RowSpace rs, VS src, AdjParams
                 Ria[a][q] = v;
             }
         // Rb = -Ri^T Rib Ri^T: Rb[x][y] = -sum_a sum_q Ri[a][x] Rib[a][q] Ri[y][q]
+        T Rb[3][3];
 #pragma unroll
         for (int x = 0; x < 3; x++)
 #pragma unroll
@@ -834,13 +860,25 @@ __global__ void __launch_bounds__(128) k_adj_vg_a(RowSpace rs, VS src, AdjParams
                 for (int a = 0; a < 3; a++)
 #pragma unroll
                     for (int q = 0; q < 3; q++) v += Ri[a][x] * Ria[a][q] * Ri[y][q];
-                out[3 * x + y] = (f64) -v;
+                Rb[x][y] = -v;
             }
-        out[27] = -kk * gdiv;
-        out[28] = -kk * gcurl[0];
-        out[29] = -kk * gcurl[1];
-        out[30] = -kk * gcurl[2];
-        out[31] = 0;
+        const T sdb = T(-kk * gdiv);
+        const T sb[3] = {T(-kk * gcurl[0]), T(-kk * gcurl[1]), T(-kk * gcurl[2])};
+        const T C[3][3] = {{0, sb[2], -sb[1]}, {-sb[2], 0, sb[0]}, {sb[1], -sb[0], 0}};
+        f64 *out = Mloc + 32 * (size_t) i;
+        out[0] = (f64) Rb[0][0];
+        out[1] = (f64) (T(0.5) * (Rb[0][1] + Rb[1][0]));
+        out[2] = (f64) (T(0.5) * (Rb[0][2] + Rb[2][0]));
+        out[3] = (f64) Rb[1][1];
+        out[4] = (f64) (T(0.5) * (Rb[1][2] + Rb[2][1]));
+        out[5] = (f64) Rb[2][2];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                out[6 + 3 * a + b]  = (f64) ((a == b ? sdb : T(0)) - Dvb[b][a] + C[a][b]);
+                out[15 + 3 * a + b] = (f64) -Dab[b][a];
+            }
         L.gal[i] = 0; // consumed
     }
 #pragma unroll
@@ -859,7 +897,7 @@ __global__ void __launch_bounds__(128) k_adj_vg_b(RowSpace rs, VS src, AdjParams
     const auto rc = src.row(c);
     const T hc = src.hrow(rc), m = T(p.pmass), sig = T(kNorm3d);
     const T ihc = T(1) / hc;
-    T Mc[31];
+    T Mc[24];
     src.mat(c, Mc);
     T gx[3] = {0, 0, 0}, gv[3] = {0, 0, 0}, gw[3] = {0, 0, 0}, gh = 0;
     const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
@@ -891,7 +929,7 @@ __global__ void __launch_bounds__(128) k_adj_vg_b(RowSpace rs, VS src, AdjParams
         if (qb < T(2)) {
             // the neighbour's term (pair (b, c) of b's sums): arguments negated, and the
             // derivative with respect to c's inputs is minus that with respect to them
-            T Mb[31];
+            T Mb[24];
             src.mat(b, Mb);
             const T ih4 = ihb * ihb * ihb * ihb;
             const T d1 = m4_d1(qb), d2 = m4_d2(qb);
@@ -937,7 +975,7 @@ __global__ void k_adj_av_stage(u32 N, u32 n, const u32 *__restrict__ sort_index,
         A32[r] = make_float4(hi32(ax), hi32(ay), hi32(az), hi32(al));
     }
 }
-// the 31 cotangents of the sums by rank (FP64, 32 per rank, or FP32, 8 float4 per rank)
+// the 24 folded cotangents of the sums by rank (FP64, 32 per rank, or FP32, 6 float4)
 __global__ void k_adj_vg_stage(u32 N, u32 n, const u32 *__restrict__ sort_index,
                                const u32 *__restrict__ ghost_src, const f64 *__restrict__ Mloc,
                                f64 *__restrict__ M64, float4 *__restrict__ M32) {
@@ -949,11 +987,11 @@ __global__ void k_adj_vg_stage(u32 N, u32 n, const u32 *__restrict__ sort_index,
     if (M64) {
         f64 *o = M64 + 32 * (size_t) r;
 #pragma unroll
-        for (int k = 0; k < 32; k++) o[k] = q[k];
+        for (int k = 0; k < 24; k++) o[k] = q[k];
     } else {
 #pragma unroll
-        for (int k = 0; k < 8; k++)
-            M32[8 * (size_t) r + k] = make_float4(hi32(q[4 * k]), hi32(q[4 * k + 1]),
+        for (int k = 0; k < 6; k++)
+            M32[6 * (size_t) r + k] = make_float4(hi32(q[4 * k]), hi32(q[4 * k + 1]),
                                                   hi32(q[4 * k + 2]), hi32(q[4 * k + 3]));
     }
 }
@@ -1101,13 +1139,16 @@ cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_loc
     f64 *Mloc = nullptr, *A64 = nullptr, *VM64 = nullptr;
     float4 *A32 = nullptr, *VM32 = nullptr;
     if (var) {
-        const size_t need = 32 * n_ + (fp32 ? 2 * N_ + 16 * N_ : 4 * N_ + 32 * N_) + 64;
+        // FP32: the A records (N float4) padded to 32 bytes, so that the folded cotangents
+        // start on the 32-byte boundary their 256-bit loads need
+        const size_t a32 = (2 * N_ + 3) & ~(size_t) 3;
+        const size_t need = 32 * n_ + (fp32 ? a32 + 12 * N_ : 4 * N_ + 32 * N_) + 64;
         if ((e = c.adj_vg.ensure(sizeof(f64) * need, s)) != cudaSuccess) return e;
         Mloc = c.adj_vg.as<f64>();
         f64 *rest = Mloc + 32 * n_;
         if (fp32) {
             A32  = (float4 *) rest;
-            VM32 = (float4 *) (rest + 2 * N_);
+            VM32 = (float4 *) (rest + a32);
         } else {
             A64  = rest;
             VM64 = rest + 4 * N_;
@@ -1162,13 +1203,16 @@ cudaError_t adjoint_backward(Ctx &c, const RowSpace &rs, u32 n, const f64 *h_loc
             ProfScope pv(c, kProfVelGrad, n);
             if (fp32) {
                 VG32 vg{P32, V32, A32, VM32};
-                { k_adj_vg_a<VG32><<<div_up(n, 128), 128, 0, s>>>(rs, vg, p, L, h_local, omega_local, Mloc, g_av); GBSPH_COUNTED; }
+                const float *taped = tape.vg_recorded
+                                         ? tape.snap_vg->as<float>() + (size_t) (k - 1) * 24 * n_
+                                         : nullptr;
+                { k_adj_vg_a<VG32><<<div_up(n, 128), 128, 0, s>>>(rs, vg, p, L, h_local, omega_local, Mloc, g_av, taped); GBSPH_COUNTED; }
                 { k_adj_vg_stage<<<gN, 256, 0, s>>>(N, n, si, gs, Mloc, nullptr, VM32); GBSPH_COUNTED; }
                 { k_adj_vg_b<VG32><<<div_up(n, 128), 128, 0, s>>>(rs, vg, p, L); GBSPH_COUNTED; }
             } else {
                 VG64 vg{rs.x, rs.y, rs.z, R, R + N_, R + 2 * N_, A64, A64 + N_, A64 + 2 * N_,
                         R + 4 * N_, VM64};
-                { k_adj_vg_a<VG64><<<div_up(n, 128), 128, 0, s>>>(rs, vg, p, L, h_local, omega_local, Mloc, g_av); GBSPH_COUNTED; }
+                { k_adj_vg_a<VG64><<<div_up(n, 128), 128, 0, s>>>(rs, vg, p, L, h_local, omega_local, Mloc, g_av, nullptr); GBSPH_COUNTED; }
                 { k_adj_vg_stage<<<gN, 256, 0, s>>>(N, n, si, gs, Mloc, VM64, nullptr); GBSPH_COUNTED; }
                 { k_adj_vg_b<VG64><<<div_up(n, 128), 128, 0, s>>>(rs, vg, p, L); GBSPH_COUNTED; }
             }

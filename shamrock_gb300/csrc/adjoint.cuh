@@ -15,6 +15,10 @@ struct StepTape {
     // varying viscosity: before each evaluation the accelerations of the last one (the
     // velocity gradients' input, 3 n) and the evaluation's switched alpha (n), local ids
     DevBuf *snap_av  = nullptr;
+    // mixed-precision varying viscosity: the velocity gradients' bare sums of each
+    // evaluation (R, Dv, Da: 24 floats per particle), so the reverse need not redo them
+    DevBuf *snap_vg  = nullptr;
+    bool vg_recorded = false; // the forward recorded them (mixed tiers)
 };
 constexpr u32 kTapeMaxIters = 16;
 

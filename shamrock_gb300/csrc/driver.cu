@@ -64,7 +64,7 @@ Ctx::~Ctx() {
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
                       &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2, &f_comp, &guard_state,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
-                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &adj_snap_av, &adj_vg, &aext, &av_arank,
+                      &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &adj_snap_av, &adj_snap_vg, &adj_vg, &aext, &av_arank,
                       &av_alpha_rank, &av_alpha_upd, &av_diag};
     cudaSetDevice(device);
     for (DevBuf *b : bufs) b->release(stream);
@@ -791,6 +791,8 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     if (tape) {
         CU(tape->snap->ensure(sizeof(f64) * 4 * (size_t) n * tape->forced_iters, s));
         if (cd10) CU(tape->snap_av->ensure(sizeof(f64) * 4 * (size_t) n * tape->forced_iters, s));
+        if (cd10 && mixed && tape->snap_vg)
+            CU(tape->snap_vg->ensure(sizeof(float) * 24 * (size_t) n * tape->forced_iters, s));
         tape->iters = 0;
     }
     HydroSpace hs{c.sh2.as<f64>(), c.su.as<f64>(),  c.svx.as<f64>(), c.svy.as<f64>(),
@@ -829,8 +831,12 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             }
             f64 *alpha_upd = c.av_alpha_upd.as<f64>();
             if (mixed) {
+                float *vg_sums = (tape && tape->snap_vg)
+                                     ? tape->snap_vg->as<float>() + (size_t) corr_iters * 24 * n
+                                     : nullptr;
                 CU(velgrad_mixed(c, rs, c.omega_local.as<f64>(), cfg->pmass, divv, cx, cy, cz, cvs,
-                                 dtdv));
+                                 dtdv, vg_sums));
+                if (vg_sums) tape->vg_recorded = true;
             } else {
                 CU(c.av_arank.ensure(sizeof(f64) * 3 * (size_t) N, s));
                 f64 *ar = c.av_arank.as<f64>();
@@ -1075,6 +1081,7 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     tape.forced_iters = corrector_iters;
     tape.snap         = &c.adj_snap;
     tape.snap_av      = &c.adj_snap_av;
+    tape.snap_vg      = &c.adj_snap_vg;
     int st = evolve_impl(ctx, &w, cfg, &ts, nullptr, &tape);
     if (st != GBSPH_OK) return st;
     RowSpace rs{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),

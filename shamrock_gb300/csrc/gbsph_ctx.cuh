@@ -164,7 +164,7 @@ struct Ctx {
     DevBuf dt_part;
 
     // ---- adjoint: working state, tape, accumulators (local and rank order)
-    DevBuf adj_state, adj_snap, adj_loc, adj_rank, adj_snap_av, adj_vg;
+    DevBuf adj_state, adj_snap, adj_loc, adj_rank, adj_snap_av, adj_snap_vg, adj_vg;
 
     ~Ctx();
 };

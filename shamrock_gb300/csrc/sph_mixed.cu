@@ -577,7 +577,8 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
                                                        f64 pmass, float mh3,
                                                        f64 *__restrict__ divv, f64 *__restrict__ cx,
                                                        f64 *__restrict__ cy, f64 *__restrict__ cz,
-                                                       u32 cvs, f64 *__restrict__ dtdivv) {
+                                                       u32 cvs, f64 *__restrict__ dtdivv,
+                                                       float *__restrict__ sums) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= rs.n) return;
     const u32 a  = rs.row_rank[t];
@@ -633,6 +634,24 @@ __global__ void __launch_bounds__(128) k_velgrad_mixed(RowSpace rs, MixedSpace m
         }
     }
     const u32 i = rs.row_local[t];
+    if (sums) {
+        // recorded for the reverse pass (by local id, 24 per row): R (xx xy xz yy yz zz),
+        // Dv and Da row-major, the bare sums (without the pair mass)
+        float *o = sums + 24 * (size_t) i;
+        o[0] = R00;
+        o[1] = R01;
+        o[2] = R02;
+        o[3] = R11;
+        o[4] = R12;
+        o[5] = R22;
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int k2 = 0; k2 < 3; k2++) {
+                o[6 + 3 * j + k2]  = Dv[j][k2];
+                o[15 + 3 * j + k2] = Da[j][k2];
+            }
+    }
     const float rho_a = mh3 * hia2 * hia;
     const float f = -(float) pmass / (__double2float_rn(omega_local[i]) * rho_a);
     divv[i] = (f64) (-f * ((Dv[0][0] + Dv[1][1]) + Dv[2][2]));
@@ -779,12 +798,13 @@ cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u
 }
 
 cudaError_t velgrad_mixed(Ctx &c, const RowSpace &rs, const f64 *omega_local, f64 pmass,
-                          f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv) {
+                          f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv,
+                          float *sums) {
     MixedSpace ms = mixed_space(c, c.n_obj);
     ProfScope ps(c, kProfVelGrad, rs.n);
     { k_velgrad_mixed<<<div_up(rs.n, 128), 128, 0, c.stream>>>(
         rs, ms, c.f_aux1.as<float4>(), omega_local, pmass, (float) (pmass * kHfact * kHfact * kHfact),
-        divv, cx, cy, cz, cvs, dtdivv); GBSPH_COUNTED; }
+        divv, cx, cy, cz, cvs, dtdivv, sums); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 

@@ -54,8 +54,11 @@ cudaError_t derivs_step_mixed(Ctx &c, const RowSpace &rs, f64 pmass, f64 alpha_u
 // varying viscosity: div v, curl v, d(div v)/dt per row (outputs by local id), after
 // gather_stage_mixed(..., true); alpha of the local particles into the records; the
 // staged plain c_s back to local order
+// sums (optional, 24 floats per row by local id): the row's bare R, Dv and Da, recorded
+// for the adjoint's reverse pass
 cudaError_t velgrad_mixed(Ctx &c, const RowSpace &rs, const f64 *omega_local, f64 pmass,
-                          f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv);
+                          f64 *divv, f64 *cx, f64 *cy, f64 *cz, u32 cvs, f64 *dtdivv,
+                          float *sums = nullptr);
 cudaError_t stage_alpha_mixed(Ctx &c, u32 N, u32 n_local, const f64 *alpha_local);
 cudaError_t cs_to_local_mixed(Ctx &c, u32 n, f64 *dst);
 // sph_comp.cu, the compensated tier: one double-float Newton step of h per row (rows
