@@ -221,13 +221,14 @@ class ClockSampler:
 # Compulsory DRAM bytes per unit of each stage (neighbour-field gathers are counted as
 # L1/L2 hits; index streams and per-particle fields are counted).  units: rows (local
 # particles), entries (CSR entries), keys (sorted slots).
-def stage_bytes(stage, n, N, entries, P, precision, h_iters):
+def stage_bytes(stage, n, N, entries, P, precision, h_iters, kept=None):
     mixed = precision.startswith("mixed")
     vec = 64 if mixed else 88
     table = {
         # row_rank, row_local, cnt, off, own fields, CSR entries, caller a/du/v/u in+out,
         # h; every particle's record read once from DRAM (further gathers: L1/L2 hits)
-        "derivs": n * (16 + vec + 128 + 8) + 4 * entries + N * vec,
+        # (entries: the rows as the derivatives read them, compacted in the FP32 tier)
+        "derivs": n * (16 + vec + 128 + 8) + 4 * (kept or entries) + N * vec,
         # per Newton iteration: CSR entries + own position + per-row h/eps state
         "h_iterate": (n * (16 + (32 if mixed else 24) + 40) + 4 * entries) * h_iters,
         "cache_fill": n * (4 + 4 + 4 + 32) + 4 * entries,
@@ -244,10 +245,12 @@ def roofline(prof, log, n, precision, peaks_path):
     dom = max(ms, key=ms.get)
     launches = prof[dom][1]
     entries = int(log["cache_size"])
+    # the entries the derivatives visit (the FP32 tier's compacted rows)
+    kept = int(log.get("cache_kept") or entries)
     N = n + int(log["n_ghost"])
     P = 1 << (N - 1).bit_length()
     h_iters = max(1, int(log["h_iterations"]))
-    nbytes = stage_bytes(dom, n, N, entries, P, precision, h_iters)
+    nbytes = stage_bytes(dom, n, N, entries, P, precision, h_iters, kept)
     peak, peak_src = 6800.0, "fallback"
     try:
         with open(peaks_path) as f:
@@ -617,6 +620,7 @@ def run_gb300(args):
         "config": {"workload": name, "precision": args.precision, "particles": n,
                    "ghosts": int(log["n_ghost"]), "leaves": int(log["leaf_count"]),
                    "cache_entries": int(log["cache_size"]),
+                   "cache_entries_in_support": int(log.get("cache_kept") or log["cache_size"]),
                    "l2": "inputs larger than L2 (fields + neighbour cache ~%d MB per step)"
                          % ((int(log["cache_size"]) * 4 + n * 200) // 2**20),
                    "parallelism": f"replicas x{world}"},

@@ -164,6 +164,9 @@ typedef struct {
      * magnitude of each field; 0 in FP64) */
     uint32_t tier, tier_reruns;
     double err_est_a, err_est_du;
+    /* neighbour-cache entries the corrector evaluations visit: the pairs inside either
+     * particle's support, which the FP32 tier compacts the rows to (cache_size otherwise) */
+    uint64_t cache_kept;
 } gbsph_step_log;
 
 /* ------------------------------------------------------------------ lifetime */

@@ -65,7 +65,8 @@ class StepLog(C.Structure):
                 ("n_local", _u32), ("n_ghost", _u32), ("leaf_count", _u32), ("h_subcycles", _u32),
                 ("h_iterations", _u32), ("corrector_iters", _u32), ("cache_size", _u64),
                 ("eps_v", _f64), ("max_eps_h", _f64), ("elapsed_s", _f64), ("rate", _f64),
-                ("tier", _u32), ("tier_reruns", _u32), ("err_est_a", _f64), ("err_est_du", _f64)]
+                ("tier", _u32), ("tier_reruns", _u32), ("err_est_a", _f64), ("err_est_du", _f64),
+                ("cache_kept", _u64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

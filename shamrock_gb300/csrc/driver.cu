@@ -877,7 +877,7 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         f64 C_cour  = cfg->cfl_cour * ts->cfl_mult;
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
         // the error estimate of the mixed tiers comes from the step's first evaluation
-        const bool cond = corr_iters == 0;
+        const bool cond = corr_iters == 0 && c.cond_this_step;
         if (comp)
             CU(derivs_step_comp(c, rs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
                                 dt / 2, C_cour, C_force, lf, ext, cd10, cond));
@@ -928,9 +928,13 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     lg.elapsed_s       = elapsed;
     lg.rate            = elapsed > 0 ? f64(n) / elapsed : 0;
     lg.tier            = tier;
-    if (mixed) {
+    lg.cache_kept      = (mixed && !comp) ? c.h_scalars->csr_kept : lg.cache_size;
+    if (mixed && c.cond_this_step) {
         lg.err_est_a  = err_estimate(c.h_scalars->cond_fa, c.h_scalars->cond_a);
         lg.err_est_du = err_estimate(c.h_scalars->cond_fu, c.h_scalars->cond_du);
+    } else if (mixed) {
+        lg.err_est_a  = c.guard_est_a; // the last refreshed estimate
+        lg.err_est_du = c.guard_est_du;
     }
     if (log) *log = lg;
     if (!converged) ctx->c.err = "the h iterator is not converged after the maximum number of "
@@ -986,17 +990,24 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     const bool av  = cfg->av_kind != GBSPH_AV_CONSTANT && p->alpha_AV && p->soundspeed;
     u32 tier       = c.guard_tier == GBSPH_MIXED_COMPENSATED ? GBSPH_MIXED_COMPENSATED : GBSPH_MIXED;
     const gbsph_time_state ts0 = *ts;
-    if (tier == GBSPH_MIXED) {
+    // The estimate is refreshed on every step while it is within a factor 8 of the
+    // tolerance; further below, on every fourth step (a state whose FP32 error is that far
+    // inside the tolerance does not reach it within a few CFL steps, and the condition
+    // sums cost their evaluation about a fifth more time).
+    const bool refresh = c.guard_skip == 0;
+    c.cond_this_step   = refresh;
+    if (tier == GBSPH_MIXED && refresh) {
         int st = save_state(ctx, p, av);
         if (st != GBSPH_OK) return st;
     }
     gbsph_step_log lg;
     std::memset(&lg, 0, sizeof(lg));
     int st = evolve_tier(ctx, p, cfg, ts, &lg, nullptr, tier);
+    c.cond_this_step = true;
     if (st != GBSPH_OK) return st;
     f64 est = std::max(lg.err_est_a, lg.err_est_du);
     u32 reruns = 0;
-    if (tier == GBSPH_MIXED && !(est <= tol)) {
+    if (tier == GBSPH_MIXED && refresh && !(est <= tol)) {
         // the FP32 tier cannot be trusted with this state: redo the step compensated
         st = restore_state(ctx, p, av);
         if (st != GBSPH_OK) return st;
@@ -1011,6 +1022,13 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     // estimate is well inside the tolerance
     c.guard_tier    = (tier == GBSPH_MIXED_COMPENSATED && !(est <= tol / 4)) ? GBSPH_MIXED_COMPENSATED
                                                                             : GBSPH_MIXED;
+    if (refresh) {
+        c.guard_est_a  = lg.err_est_a;
+        c.guard_est_du = lg.err_est_du;
+        c.guard_skip   = (tier == GBSPH_MIXED && est <= tol / 8) ? 3 : 0;
+    } else {
+        c.guard_skip--;
+    }
     lg.tier_reruns  = reruns;
     lg.elapsed_s    = std::chrono::duration<f64>(std::chrono::steady_clock::now() - t0).count();
     lg.rate         = lg.elapsed_s > 0 ? f64(p->n) / lg.elapsed_s : 0;

@@ -29,6 +29,7 @@ struct Scalars {
     u64 dt_min;        // ordered-u64 min of per-particle CFL dt
     u64 n_unconverged; // particles whose per-thread iteration cap was hit
     u64 csr_entries;   // stage-2 entries of the one-pass cache build
+    u64 csr_kept;      // entries kept by the mixed path's row compaction
     u64 cond_fa;       // ordered-u64 max over rows of the force condition sum (mixed)
     u64 cond_fu;       // ordered-u64 max of the du/dt condition sum
     u64 cond_a;        // ordered-u64 max |bare hydro force sum|
@@ -153,6 +154,11 @@ struct Ctx {
     // error-controlled mixed precision: the tier the next step starts in (1 FP32 pair
     // arithmetic, 2 compensated) and the start state a step is recomputed from
     u32 guard_tier = 1;
+    // steps left before the FP32 tier's error estimate is refreshed (0: this step), and the
+    // last estimate (a, du/dt); see evolve_impl
+    u32 guard_skip = 0;
+    f64 guard_est_a = 0, guard_est_du = 0;
+    bool cond_this_step = true;
     DevBuf guard_state;
 
     // ---- per-row / per-local work arrays

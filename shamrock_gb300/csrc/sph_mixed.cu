@@ -302,57 +302,62 @@ __global__ void k_restage_hinv(const u32 *__restrict__ sort_index, u32 N, u32 n_
 __global__ void __launch_bounds__(256) k_omega_compact_mixed(RowSpace rs, MixedSpace ms,
                                                              const f64 *__restrict__ h_row,
                                                              f64 *__restrict__ omega_local,
-                                                             u32 *ent_w, u32 *cnt_w) {
+                                                             u32 *ent_w, u32 *cnt_w, Scalars *sc) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= rs.n) return;
-    const u32 a  = rs.row_rank[t];
-    const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
-    const float hinv  = __double2float_rn(rcp64(h_row[t]));
-    const float hinv2 = hinv * hinv;
-    const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
-    float sg = 0.f, cg = 0.f;
-    // kept entries are collected four at a time and written with one 128-bit store
-    // (rows start on 16-byte boundaries and their slots are padded to four entries)
-    u32 w = k0, p = 0;
-    uint4 pend = make_uint4(a, a, a, a);
-    uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, true, a) : make_uint4(a, a, a, a);
-    for (u32 k = k0; k < k1; k += 4) {
-        const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
-        F8 pb[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) pb[j] = ldg256(&ms.P[2 * (size_t) bb[j]]);
-        if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, true, a);
-        float bg = 0.f;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (k + j >= k1) continue;
-            float dx = (pa.a.x - pb[j].a.x) + (pa.b.x - pb[j].b.x);
-            float dy = (pa.a.y - pb[j].a.y) + (pa.b.y - pb[j].b.y);
-            float dz = (pa.a.z - pb[j].a.z) + (pa.b.z - pb[j].b.z);
-            float r2 = dx * dx + dy * dy + dz * dz;
-            const float hib = pb[j].a.w;
-            if (!(r2 * hinv2 > 4.f && r2 * (hib * hib) > 4.f)) {
-                const u32 b = bb[j];
-                pend.x = p == 0 ? b : pend.x;
-                pend.y = p == 1 ? b : pend.y;
-                pend.z = p == 2 ? b : pend.z;
-                pend.w = p == 3 ? b : pend.w;
-                if (++p == 4) {
-                    *(uint4 *) (ent_w + w) = pend;
-                    w += 4;
-                    p = 0;
+    u64 kept = 0;
+    if (t < rs.n) {
+        const u32 a  = rs.row_rank[t];
+        const u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
+        const float hinv  = __double2float_rn(rcp64(h_row[t]));
+        const float hinv2 = hinv * hinv;
+        const F8 pa = ldg256(&ms.P[2 * (size_t) a]);
+        float sg = 0.f, cg = 0.f;
+        // kept entries are collected four at a time and written with one 128-bit store
+        // (rows start on 16-byte boundaries and their slots are padded to four entries)
+        u32 w = k0, p = 0;
+        uint4 pend = make_uint4(a, a, a, a);
+        uint4 nx = (k0 < k1) ? load_entries(rs.ent, k0, k1, true, a) : make_uint4(a, a, a, a);
+        for (u32 k = k0; k < k1; k += 4) {
+            const u32 bb[4] = {nx.x, nx.y, nx.z, nx.w};
+            F8 pb[4];
+    #pragma unroll
+            for (int j = 0; j < 4; j++) pb[j] = ldg256(&ms.P[2 * (size_t) bb[j]]);
+            if (k + 4 < k1) nx = load_entries(rs.ent, k + 4, k1, true, a);
+            float bg = 0.f;
+    #pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (k + j >= k1) continue;
+                float dx = (pa.a.x - pb[j].a.x) + (pa.b.x - pb[j].b.x);
+                float dy = (pa.a.y - pb[j].a.y) + (pa.b.y - pb[j].b.y);
+                float dz = (pa.a.z - pb[j].a.z) + (pa.b.z - pb[j].b.z);
+                float r2 = dx * dx + dy * dy + dz * dz;
+                const float hib = pb[j].a.w;
+                if (!(r2 * hinv2 > 4.f && r2 * (hib * hib) > 4.f)) {
+                    const u32 b = bb[j];
+                    pend.x = p == 0 ? b : pend.x;
+                    pend.y = p == 1 ? b : pend.y;
+                    pend.z = p == 2 ? b : pend.z;
+                    pend.w = p == 3 ? b : pend.w;
+                    if (++p == 4) {
+                        *(uint4 *) (ent_w + w) = pend;
+                        w += 4;
+                        p = 0;
+                    }
                 }
+                float q2 = r2 * hinv2;
+                if (q2 > 4.f) continue;
+                float q = sqrt_approx(q2);
+                bg += 3.f * m4_f32(q) + q * m4_df32(q);
             }
-            float q2 = r2 * hinv2;
-            if (q2 > 4.f) continue;
-            float q = sqrt_approx(q2);
-            bg += 3.f * m4_f32(q) + q * m4_df32(q);
+            kahan_add(sg, cg, bg);
         }
-        kahan_add(sg, cg, bg);
+        if (p) *(uint4 *) (ent_w + w) = pend; // the tail (slots past it hold stale entries)
+        cnt_w[t] = w - k0 + p;
+        kept     = w - k0 + p;
+        omega_local[rs.row_local[t]] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
     }
-    if (p) *(uint4 *) (ent_w + w) = pend; // the tail (slots past it hold stale entries)
-    cnt_w[t] = w - k0 + p;
-    omega_local[rs.row_local[t]] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
+    kept = block_reduce(kept, OpAddU64{}, 0ull);
+    if (threadIdx.x == 0) atomicAdd((unsigned long long *) &sc->csr_kept, (unsigned long long) kept);
 }
 
 // FP32 pair loop of the constant-AV derivatives; returns the bare sums
@@ -439,14 +444,16 @@ __device__ __forceinline__ void derivs_row_f32(const RowSpace &rs, const MixedSp
             bx += f * dx;
             by += f * dy;
             bz += f * dz;
+            // the two du/dt terms rounded explicitly (no contraction, no sharing with the
+            // force products), so that the instantiations with and without the condition
+            // sums give the same bits
+            const float tp = __fmul_rn(__fmul_rn(__fmul_rn(AVPa, c1a), Fa), vr);
+            const float tc = __fmul_rn(__fmul_rn(0.5f * p.alpha_u, vsig_u),
+                                       __fadd_rn(__fmul_rn(Fa, c2a), __fmul_rn(Fb, c2b)));
+            bu += tp + tc * (u_a - hb[j].a.w);
             if (COND) {
-                const float tp = AVPa * c1a * Fa * vr;
-                const float tc = 0.5f * p.alpha_u * vsig_u * (Fa * c2a + Fb * c2b);
-                bu += tp + tc * (u_a - hb[j].a.w);
                 sa += fabsf(pf);
                 su += fabsf(tp) + fabsf(tc) * (abs_ua + fabsf(hb[j].a.w));
-            } else {
-                bu += AVPa * c1a * Fa * vr + 0.5f * p.alpha_u * vsig_u * (u_a - hb[j].a.w) * (Fa * c2a + Fb * c2b);
             }
             vsig_max = fmaxf(vsig_max, cs_sig + 2.f * avr);
         }
@@ -747,7 +754,8 @@ cudaError_t omega_compact_mixed(Ctx &c, const RowSpace &rs, u32 N, u32 n_local, 
                                                          c.ghost_src.as<u32>(), h_local,
                                                          c.f_pos.as<float4>()); GBSPH_COUNTED; }
     { k_omega_compact_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(
-        rs, ms, h_row, omega_local, c.csr_ent.as<u32>(), c.csr_cnt.as<u32>()); GBSPH_COUNTED; }
+        rs, ms, h_row, omega_local, c.csr_ent.as<u32>(), c.csr_cnt.as<u32>(),
+        c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
     // the cache no longer holds the reference's pair set
     c.cache_valid = false;
     return cudaGetLastError();
