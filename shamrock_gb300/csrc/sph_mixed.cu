@@ -263,20 +263,6 @@ __global__ void __launch_bounds__(256, 4) k_h_iterate_mixed(RowSpace rs, MixedSp
     }
 }
 
-__global__ void __launch_bounds__(256) k_omega_mixed(RowSpace rs, MixedSpace ms,
-                                                     const f64 *__restrict__ h_row, f64 pmass,
-                                                     f64 *__restrict__ omega_local) {
-    u32 t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= rs.n) return;
-    u32 a  = rs.row_rank ? rs.row_rank[t] : t;
-    u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
-    float sf, sg;
-    density_sums_f32(rs, ms, a, k0, k1, __double2float_rn(rcp64(h_row[t])), sf, sg);
-    // Omega = 1 + h / (3 rho_h) drho/dh = 1 + B / 3, B = -kNorm3d / hfact^3 sum (3f + q f')
-    omega_local[rs.row_local ? rs.row_local[t] : t] = (f64) (1.f - kDensRatio * sg * (1.f / 3.f));
-}
-
-
 // 1/h lane of the position records from the converged smoothing lengths (the records
 // were staged with the h the neighbour cache was built with); the same value the
 // corrector staging writes, so the compaction below and the corrector kernels test
@@ -291,8 +277,9 @@ __global__ void k_restage_hinv(const u32 *__restrict__ sort_index, u32 N, u32 n_
     ((float *) &P[2 * (size_t) r])[3] = __double2float_rn(rcp64(h[src]));
 }
 
-// Omega (as k_omega_mixed) and, in the same pass over the row, the row compacted in
-// place to the entries the corrector kernels can use: pairs inside either particle's
+// Omega = 1 + B / 3, B = -kNorm3d / hfact^3 sum (3f + q f') (ComputeOmega.cpp:36-73 in
+// the dimensionless form of the FP32 h iteration) and, in the same pass over the row,
+// the row compacted in place to the entries the corrector kernels can use: pairs inside either particle's
 // support at the converged h, the test of derivs_row_f32 (r^2 h_a^-2 > 4 and
 // r^2 h_b^-2 > 4 drops a pair), coincident pairs and the particle itself kept (the
 // density terms of the reverse pass include them).  About a quarter of a row lies
@@ -736,13 +723,6 @@ cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h
     { k_h_iterate_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(
         rs, ms, h_old, h_new, eps, pmass, h_evol_max, h_evol_iter_max, iters, eps_p,
         c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
-    return cudaGetLastError();
-}
-
-cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local) {
-    ProfScope ps(c, kProfOmega, rs.n);
-    MixedSpace ms = mixed_space(c, c.n_obj);
-    { k_omega_mixed<<<div_up(rs.n, 256), 256, 0, c.stream>>>(rs, ms, h_row, pmass, omega_local); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 

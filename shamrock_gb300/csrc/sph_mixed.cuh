@@ -27,7 +27,6 @@ const float4 *mixed_positions(Ctx &c);
 cudaError_t h_iterate_mixed(Ctx &c, const RowSpace &rs, const f64 *h_old, f64 *h_new, f64 *eps,
                             f64 pmass, f64 h_evol_max, f64 h_evol_iter_max, u32 iters,
                             f64 eps_p = 1e-6);
-cudaError_t omega_mixed(Ctx &c, const RowSpace &rs, const f64 *h_row, f64 pmass, f64 *omega_local);
 // the pipeline's Omega: restages the records' 1/h from the converged h (local ids), then
 // Omega per row and, in the same pass, each cache row compacted in place to the pairs
 // inside either support (the entries the corrector kernels visit); the cache is no
