@@ -458,6 +458,7 @@ def precision_control(logs):
             "steps_compensated": sum(1 for g in logs if g["tier"] == 2),
             "steps_fp64": sum(1 for g in logs if g["tier"] == 0),
             "reruns": sum(int(g["tier_reruns"]) for g in logs),
+            "estimate_refreshes": sum(int(g.get("est_refreshed", 1)) for g in logs),
             "compensated_fraction": sum(1 for g in logs if g["tier"] == 2) / n,
             "fp32_err_est_max": {"a": max(g["err_est_a"] for g in logs) if logs else None,
                                  "du_dt": max(g["err_est_du"] for g in logs) if logs else None},
@@ -465,7 +466,8 @@ def precision_control(logs):
                           "arithmetic while the estimated error of the FP32 tier stays within "
                           "1e-5, else the compensated tier; a rerun recomputes a step that "
                           "started in FP32 compensated); estimates relative to each field's "
-                          "largest magnitude"}
+                          "largest magnitude, refreshed on every fourth step where they cannot "
+                          "reach the tolerance in the steps between"}
 
 
 def accuracy(s, alpha_AV=1.0, precision="mixed"):
@@ -522,6 +524,18 @@ def oracle_parity(first, alpha_AV, precision):
     diff += ["log." + k for k in PARITY_KEYS if l64[k] != first["log"][k]]
     out["fp64_bitexact"] = not diff
     out["fp64_mismatches"] = diff
+    # the largest difference of each mismatched field, relative to the field's largest
+    # magnitude (e.g. the LP07 sound speed, whose power function the GPU and the host C
+    # library each round in their own way)
+    maxrel = {}
+    for k in diff:
+        if k.startswith("log."):
+            continue
+        x = np.asarray(g[k])
+        y = np.asarray(o[k] if k in PARITY_FIELDS else first["av"][k])
+        maxrel[k] = float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+    if maxrel:
+        out["fp64_max_rel_diff"] = maxrel
     del m64
     mm = make_model(s, precision, alpha_AV=alpha_AV)
     lm = mm.evolve_once()

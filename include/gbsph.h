@@ -51,8 +51,10 @@ extern "C" {
  * the FP32 tier from condition sums the derivatives pass accumulates (the summed pair
  * force and du/dt magnitudes against the largest result); a step whose estimate exceeds
  * gbsph_config.mixed_tol is recomputed from its start state in the compensated tier, and
- * later steps stay there until the estimate falls below a quarter of the tolerance.
- * gbsph_step_log reports the tier, reruns and estimates. */
+ * later steps stay there until the estimate falls below a quarter of the tolerance.  The
+ * estimate is refreshed on every fourth step where it cannot reach the tolerance in the
+ * steps between (below an eighth of it, or below 0.8 of it and growing slowly enough),
+ * else on every step.  gbsph_step_log reports the tier, reruns and estimates. */
 #define GBSPH_MIXED_GUARDED 3
 
 typedef struct gbsph_ctx gbsph_ctx;
@@ -167,6 +169,10 @@ typedef struct {
     /* neighbour-cache entries the corrector evaluations visit: the pairs inside either
      * particle's support, which the FP32 tier compacts the rows to (cache_size otherwise) */
     uint64_t cache_kept;
+    /* GBSPH_MIXED_GUARDED: 1 when this step refreshed the error estimate (its first
+     * corrector evaluation accumulated the condition sums), 0 when it reports the last
+     * refreshed one; 1 in the other precisions */
+    uint32_t est_refreshed, pad4;
 } gbsph_step_log;
 
 /* ------------------------------------------------------------------ lifetime */

@@ -66,7 +66,7 @@ class StepLog(C.Structure):
                 ("h_iterations", _u32), ("corrector_iters", _u32), ("cache_size", _u64),
                 ("eps_v", _f64), ("max_eps_h", _f64), ("elapsed_s", _f64), ("rate", _f64),
                 ("tier", _u32), ("tier_reruns", _u32), ("err_est_a", _f64), ("err_est_du", _f64),
-                ("cache_kept", _u64)]
+                ("cache_kept", _u64), ("est_refreshed", _u32), ("pad4", _u32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

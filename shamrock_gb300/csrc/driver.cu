@@ -929,6 +929,7 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     lg.rate            = elapsed > 0 ? f64(n) / elapsed : 0;
     lg.tier            = tier;
     lg.cache_kept      = (mixed && !comp) ? c.h_scalars->csr_kept : lg.cache_size;
+    lg.est_refreshed   = c.cond_this_step ? 1 : 0;
     if (mixed && c.cond_this_step) {
         lg.err_est_a  = err_estimate(c.h_scalars->cond_fa, c.h_scalars->cond_a);
         lg.err_est_du = err_estimate(c.h_scalars->cond_fu, c.h_scalars->cond_du);
@@ -985,15 +986,22 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
                        "(gbsph_step_log.tier), not in GBSPH_MIXED_GUARDED");
     REQUIRE_ARG(p->n > 0, "empty patch");
     Ctx &c = ctx->c;
+    if (p->xyz.x != c.guard_of || p->n != c.guard_n) {
+        // other particle arrays: their estimate starts afresh, in the FP32 tier
+        c.guard_of = p->xyz.x, c.guard_n = p->n;
+        c.guard_tier = GBSPH_MIXED, c.guard_skip = 0, c.guard_prev_est = -1, c.guard_since = 0;
+    }
     auto t0        = std::chrono::steady_clock::now();
     const f64 tol  = cfg->mixed_tol > 0 ? cfg->mixed_tol : 1e-5;
     const bool av  = cfg->av_kind != GBSPH_AV_CONSTANT && p->alpha_AV && p->soundspeed;
     u32 tier       = c.guard_tier == GBSPH_MIXED_COMPENSATED ? GBSPH_MIXED_COMPENSATED : GBSPH_MIXED;
     const gbsph_time_state ts0 = *ts;
-    // The estimate is refreshed on every step while it is within a factor 8 of the
-    // tolerance; further below, on every fourth step (a state whose FP32 error is that far
-    // inside the tolerance does not reach it within a few CFL steps, and the condition
-    // sums cost their evaluation about a fifth more time).
+    // The estimate is refreshed on every fourth step when it cannot reach the tolerance in
+    // the three steps between: when it is below an eighth of the tolerance, or below 0.8 of
+    // it and, grown at twice its rate between the last two refreshes, stays there for four
+    // steps (the condition sums follow the pressure and velocity fields, which a CFL step
+    // changes by a fraction; and the sums cost their evaluation about a third more time).
+    // Otherwise, and after any step that ran compensated, on every step.
     const bool refresh = c.guard_skip == 0;
     c.cond_this_step   = refresh;
     if (tier == GBSPH_MIXED && refresh) {
@@ -1022,13 +1030,22 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     // estimate is well inside the tolerance
     c.guard_tier    = (tier == GBSPH_MIXED_COMPENSATED && !(est <= tol / 4)) ? GBSPH_MIXED_COMPENSATED
                                                                             : GBSPH_MIXED;
+    c.guard_since++;
     if (refresh) {
         c.guard_est_a  = lg.err_est_a;
         c.guard_est_du = lg.err_est_du;
-        c.guard_skip   = (tier == GBSPH_MIXED && est <= tol / 8) ? 3 : 0;
+        bool skip = tier == GBSPH_MIXED && est <= tol / 8;
+        if (tier == GBSPH_MIXED && !skip && c.guard_prev_est >= 0 && est <= 0.8 * tol) {
+            const f64 rate = std::max(0.0, est - c.guard_prev_est) / f64(c.guard_since);
+            skip = est + 2 * 4 * rate <= 0.8 * tol;
+        }
+        c.guard_skip     = skip ? 3 : 0;
+        c.guard_prev_est = tier == GBSPH_MIXED ? est : -1;
+        c.guard_since    = 0;
     } else {
         c.guard_skip--;
     }
+    lg.est_refreshed = refresh ? 1 : 0;
     lg.tier_reruns  = reruns;
     lg.elapsed_s    = std::chrono::duration<f64>(std::chrono::steady_clock::now() - t0).count();
     lg.rate         = lg.elapsed_s > 0 ? f64(p->n) / lg.elapsed_s : 0;

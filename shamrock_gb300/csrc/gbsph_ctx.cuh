@@ -154,10 +154,15 @@ struct Ctx {
     // error-controlled mixed precision: the tier the next step starts in (1 FP32 pair
     // arithmetic, 2 compensated) and the start state a step is recomputed from
     u32 guard_tier = 1;
-    // steps left before the FP32 tier's error estimate is refreshed (0: this step), and the
-    // last estimate (a, du/dt); see evolve_impl
+    // steps left before the FP32 tier's error estimate is refreshed (0: this step), the
+    // last estimate (a, du/dt), and the refresh before it with the steps between the two
+    // (its growth rate; guard_prev_est < 0: none); see evolve_impl
     u32 guard_skip = 0;
     f64 guard_est_a = 0, guard_est_du = 0;
+    f64 guard_prev_est = -1;
+    u32 guard_since = 0;
+    const f64 *guard_of = nullptr; // the position array and count the state is for
+    u32 guard_n = 0;
     bool cond_this_step = true;
     DevBuf guard_state;
 

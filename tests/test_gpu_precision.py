@@ -117,3 +117,63 @@ def test_sedov_guarded_stays_fp32(n_cells):
             # from the same state, the estimate bounds the error it stands for
             e = _errors(dg, m64.collect_data())
             assert e["a"][0] <= lg["err_est_a"] and e["du"][0] <= max(lg["err_est_du"], 1e-7), (e, lg)
+
+
+def _refresh_replay(logs, tol):
+    """The refresh rule of the error-controlled precision, replayed from the step logs:
+    every fourth step when the last refreshed estimate lies below tol / 8, or below 0.8 tol
+    with its growth since the refresh before it, doubled over four steps, staying there;
+    else every step.  Returns the number of steps that skipped the refresh."""
+    skip_left, prev, since, skipped = 0, None, 0, 0
+    for i, lg in enumerate(logs):
+        assert lg["est_refreshed"] == (1 if skip_left == 0 else 0), (i, lg)
+        since += 1
+        if lg["est_refreshed"]:
+            est = max(lg["err_est_a"], lg["err_est_du"])
+            fp32 = lg["tier"] == 1
+            skip = fp32 and est <= tol / 8
+            if fp32 and not skip and prev is not None and est <= 0.8 * tol:
+                skip = est + 8 * max(0.0, est - prev) / since <= 0.8 * tol
+            skip_left, prev, since = (3 if skip else 0), (est if fp32 else None), 0
+        else:
+            skipped += 1
+            skip_left -= 1
+    return skipped
+
+
+def test_refresh_rule_near_tolerance():
+    """With the tolerance set at 1.6 times the Sedov blast's first estimate (not below an
+    eighth of it), the estimate is refreshed on the first steps, then every fourth step
+    while it grows slowly; the skipped steps give the FP32 tier's results bit for bit."""
+    from shamrock_gb300 import setups
+
+    s = setups.sedov_taylor(10, jitter=0.05, seed=1)
+    m32 = _model(s, "mixed_fp32", 1.0)
+    probe = _model(s, "mixed_fp32", 1.0)
+    l0 = probe.evolve_once()
+    tol = 1.6 * max(l0["err_est_a"], l0["err_est_du"])
+    mg = _model(s, "mixed", 1.0)
+    mg.get_solver_config().set_precision("mixed", tol=tol)
+    logs = []
+    for step in range(10):
+        m32.evolve_once()
+        lg = mg.evolve_once()
+        logs.append(lg)
+        if lg["tier"] == 1 and lg["tier_reruns"] == 0 and all(g["tier"] == 1 for g in logs):
+            d32, dg = m32.collect_data(), mg.collect_data()
+            for k in ("xyz", "vxyz", "axyz", "hpart", "uint", "duint"):
+                assert np.array_equal(d32[k], dg[k]), (step, k)
+    assert logs[0]["est_refreshed"] == 1 and logs[1]["est_refreshed"] == 1
+    assert _refresh_replay(logs, tol) >= 3, logs
+
+
+@pytest.mark.parametrize("n_cells", [10])
+def test_sedov_refresh_every_fourth_step(n_cells):
+    """Far below the tolerance the estimate is refreshed on steps 0, 4, 8, ..."""
+    from shamrock_gb300 import setups
+
+    s = setups.sedov_taylor(n_cells, jitter=0.05, seed=1)
+    mg = _model(s, "mixed", 1.0)
+    logs = [mg.evolve_once() for _ in range(9)]
+    assert [g["est_refreshed"] for g in logs] == [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    assert _refresh_replay(logs, TOL) == 6
