@@ -359,6 +359,21 @@ __global__ void __launch_bounds__(128) k_derivs_step(RowSpace rs, HydroSpace hs,
 }
 
 // leapfrog predictor (half kick, drift, half kick) + periodic wrap, one pass
+// fmod(r, d) for d > 0.  fmod is exact (its result is r - n d, which is representable),
+// so any exact evaluation gives the same bits: within one period of the box, the
+// remainder is r itself or r -+ d (exact by Sterbenz's lemma: d <= |r| <= 2 d); further
+// out, and for NaN or infinities, the library fmod decides.  A zero result takes the sign
+// of r, as fmod's does.
+__device__ __forceinline__ f64 fmod_wrap(f64 r, f64 d) {
+    if (fabs(r) < d) return r;
+    if (r >= d && r < 2 * d) return r - d;
+    if (r <= -d && r > -2 * d) {
+        const f64 t = r + d;
+        return t == 0 ? -0.0 : t;
+    }
+    return fmod(r, d);
+}
+
 __global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f64 b1, f64 b2,
                           f64 e0, f64 e1, f64 e2, f64 mGM, f64 *__restrict__ ext_x,
                           f64 *__restrict__ ext_y, f64 *__restrict__ ext_z) {
@@ -391,9 +406,9 @@ __global__ void k_predict(LocalFields lf, u32 n, f64 dt, int periodic, f64 b0, f
         for (int c = 0; c < 3; c++) {
             f64 delt = bmax[c] - bmin[c];
             f64 r    = p[c] - bmin[c];
-            r        = fmod(r, delt);
+            r        = fmod_wrap(r, delt);
             r += delt;
-            r = fmod(r, delt);
+            r = fmod_wrap(r, delt);
             r += bmin[c];
             p[c] = r;
         }

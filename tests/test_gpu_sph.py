@@ -176,6 +176,38 @@ def test_kdk_predict_vs_oracle(gctx, periodic):
     assert np.array_equal(uu.cpu().numpy(), ou)
 
 
+def test_kdk_predict_wrap_edges_vs_oracle(gctx):
+    """The periodic wrap (two fmods around a shift by the box size) at its edge cases:
+    positions exactly on the box faces and on whole periods from them, just inside and
+    outside, several periods away, and a box not anchored at the origin; bit for bit
+    against the oracle's std::fmod."""
+    from shamrock_gb300 import modules as M
+
+    bmin, bmax = np.array([-0.6, -0.25, 0.1]), np.array([0.6, 0.35, 1.3])
+    d = bmax - bmin
+    offs = [0.0, 1e-300, -1e-300, 1e-17, -1e-17, 0.3, -0.3, 1.0, -1.0, 2.0, -2.0, 1.0 + 1e-16,
+            -1.0 - 1e-16, 2.0 - 1e-16, -2.0 + 1e-16, 1.5, -1.5, 3.7, -3.7, 7.0, -7.0, 0.999999999,
+            -0.999999999, np.nextafter(1.0, 0), np.nextafter(-1.0, 0), np.nextafter(2.0, 3)]
+    rng = np.random.default_rng(5)
+    pts = []
+    for o in offs:
+        for c in range(3):
+            p = bmin + rng.random(3) * d
+            p[c] = bmin[c] + o * d[c]
+            pts.append(p)
+            q = bmin + rng.random(3) * d
+            q[c] = bmax[c] + o * d[c]
+            pts.append(q)
+    pos = np.array(pts)
+    n = len(pos)
+    zero = np.zeros((n, 3))
+    u, du = np.ones(n), np.zeros(n)
+    x, vv, uu = M.kdk_predict(gctx, pos, zero, u, zero, du, 0.0, True, tuple(bmin), tuple(bmax))
+    ox, ov, ou = O.predict(pos, zero, u, zero, du, 0.0, True, list(bmin), list(bmax))
+    gx = x.T.cpu().numpy()
+    assert np.array_equal(gx.view(np.uint64), ox.view(np.uint64))
+
+
 def test_kdk_correct_and_cfl_vs_oracle(gctx):
     from shamrock_gb300 import modules as M
 
