@@ -877,7 +877,9 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         f64 C_cour  = cfg->cfl_cour * ts->cfl_mult;
         f64 C_force = cfg->cfl_force * ts->cfl_mult;
         // the error estimate of the mixed tiers comes from the step's first evaluation
-        const bool cond = corr_iters == 0 && c.cond_this_step;
+        // the condition sums feed the error estimate; the adjoint's recomputation of a
+        // recorded step (tape) has no use for them
+        const bool cond = corr_iters == 0 && c.cond_this_step && !tape;
         if (comp)
             CU(derivs_step_comp(c, rs, cfg->pmass, cfg->alpha_u, cfg->alpha_AV, cfg->beta_AV,
                                 dt / 2, C_cour, C_force, lf, ext, cd10, cond));
@@ -929,8 +931,8 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     lg.rate            = elapsed > 0 ? f64(n) / elapsed : 0;
     lg.tier            = tier;
     lg.cache_kept      = (mixed && !comp) ? c.h_scalars->csr_kept : lg.cache_size;
-    lg.est_refreshed   = c.cond_this_step ? 1 : 0;
-    if (mixed && c.cond_this_step) {
+    lg.est_refreshed   = (c.cond_this_step && !tape) ? 1 : 0;
+    if (mixed && c.cond_this_step && !tape) {
         lg.err_est_a  = err_estimate(c.h_scalars->cond_fa, c.h_scalars->cond_a);
         lg.err_est_du = err_estimate(c.h_scalars->cond_fu, c.h_scalars->cond_du);
     } else if (mixed) {
