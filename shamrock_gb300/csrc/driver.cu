@@ -62,7 +62,7 @@ Ctx::~Ctx() {
                       &row_local, &row_flags, &row_offsets, &leaf_cnt, &leaf_off, &leaf_ent,
                       &owner, &leaf_thr, &csr_cnt, &csr_off, &csr_ent, &ghost_src, &ghost_oid,
                       &ghost_block_counts, &mx, &my, &mz, &mh, &d_ghost_offsets, &su, &svx, &svy,
-                      &svz, &som, &sP, &scs, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2, &f_comp, &guard_state,
+                      &svz, &som, &sP, &scs, &srho, &sinv, &srom, &sh2, &f_pos, &f_anchor, &f_aux0, &f_aux1, &f_aux2, &f_comp, &guard_state,
                       &h_old_row, &eps_row, &omega_local, &a_old, &du_old, &hnew_row, &omega_row,
                       &dt_part, &adj_state, &adj_snap, &adj_loc, &adj_rank, &adj_snap_av, &adj_snap_vg, &adj_vg, &aext, &av_arank,
                       &av_alpha_rank, &av_alpha_upd, &av_diag};
@@ -708,12 +708,10 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
         CU(tree_build(c, c.mx.as<f64>(), c.my.as<f64>(), c.mz.as<f64>(), c.mh.as<f64>(), N,
                       cfg->tree_reduction_level, cfg->htol_up_coarse, 32, 0, true));
         CU(build_rows(c, n));
-        if (mixed) {
-            CU(stage_positions_mixed(c, N, cfg->htol_up_coarse));
-            CU(neigh_cache_build(c, cfg->htol_up_coarse, mixed_positions(c)));
-        } else {
-            CU(neigh_cache_build(c, cfg->htol_up_coarse));
-        }
+        // both precisions pre-test the pairs in FP32 (exact FP64 test inside the rounding
+        // band): the cache is the FP64 one either way
+        CU(stage_positions_mixed(c, N, cfg->htol_up_coarse));
+        CU(neigh_cache_build(c, cfg->htol_up_coarse, mixed_positions(c)));
         rs = RowSpace{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
                       c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
                       c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
@@ -783,7 +781,8 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     // ---- corrector loop (Solver.cpp:2247-3171)
     // FP64 rank-ordered hydro copies (the mixed path stages 32-byte records and keeps
     // only h in FP64)
-    DevBuf *rank_bufs[] = {&c.sh2, &c.su, &c.svx, &c.svy, &c.svz, &c.som, &c.sP, &c.scs};
+    DevBuf *rank_bufs[] = {&c.sh2, &c.su,  &c.svx,  &c.svy, &c.svz, &c.som,
+                           &c.sP,  &c.scs, &c.srho, &c.sinv, &c.srom};
     for (DevBuf *b : rank_bufs) {
         CU(b->ensure(8 * (size_t) N, s));
         if (mixed) break;
@@ -797,6 +796,11 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     }
     HydroSpace hs{c.sh2.as<f64>(), c.su.as<f64>(),  c.svx.as<f64>(), c.svy.as<f64>(),
                   c.svz.as<f64>(), c.som.as<f64>(), c.sP.as<f64>(),  c.scs.as<f64>()};
+    if (!mixed) {
+        hs.rho    = c.srho.as<f64>();
+        hs.inv_sub = c.sinv.as<f64>();
+        hs.rho_om = c.srom.as<f64>();
+    }
     f64 next_cfl   = 0;
     bool rerun     = false;
     u32 corr_iters = 0;

@@ -149,6 +149,7 @@ struct Ctx {
 
     // ---- per-step fields in rank order (corrector phase)
     DevBuf su, svx, svy, svz, som, sP, scs, sh2;
+    DevBuf srho, sinv, srom; // FP64 pair-loop factors per merged particle (HydroSpace)
     // mixed precision staging (rank order); f_comp: the compensated tier's extra records
     DevBuf f_pos, f_anchor, f_aux0, f_aux1, f_aux2, f_comp;
     // error-controlled mixed precision: the tier the next step starts in (1 FP32 pair

@@ -150,7 +150,8 @@ __global__ void k_gather_eos(const u32 *__restrict__ sort_index, u32 N, u32 n_lo
                              const f64 *__restrict__ sz,
                              f64 *__restrict__ sh, f64 *__restrict__ su, f64 *__restrict__ svx,
                              f64 *__restrict__ svy, f64 *__restrict__ svz, f64 *__restrict__ som,
-                             f64 *__restrict__ sP, f64 *__restrict__ scs) {
+                             f64 *__restrict__ sP, f64 *__restrict__ scs, f64 *__restrict__ srho,
+                             f64 *__restrict__ sinv, f64 *__restrict__ srom) {
     u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
     u32 id  = sort_index[r];
@@ -161,8 +162,15 @@ __global__ void k_gather_eos(const u32 *__restrict__ sort_index, u32 N, u32 n_lo
     svx[r] = vx[(size_t) src * vs];
     svy[r] = vy[(size_t) src * vs];
     svz[r] = vz[(size_t) src * vs];
-    som[r] = omega[src];
+    const f64 om = omega[src];
+    som[r] = om;
     f64 rho = rho_h(pmass, hh);
+    if (srho) {
+        // the pair loop's per-neighbour factors, in its own expressions (derivs_row)
+        srho[r] = rho;
+        sinv[r] = inv_sat_zero((rho * rho) * om);
+        srom[r] = rho * om;
+    }
     if (eos.kind == 1) {
         // LP07 at the merged (rank-ordered) position
         f64 x = sx[r], y = sy[r], z = sz[r];
@@ -208,7 +216,11 @@ struct DerivParams {
     ExtAccel ext;        // external acceleration added to the hydro one (may be null)
 };
 
-template<bool VSIG>
+// PRE: the neighbour's rho, inv_sat_zero(rho^2 Omega) and rho Omega are read from the
+// staged per-particle factors (hs.rho, hs.inv_sub, hs.rho_om) instead of recomputed per
+// pair: the same expressions evaluated once, so the same bits, and two FP64 divisions and
+// five multiplications fewer per pair on GB300's scarce FP64 pipe.
+template<bool VSIG, bool PRE = false>
 __device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace &hs, u32 a, u32 k0,
                                            u32 k1, const DerivParams &p, f64 &fx, f64 &fy, f64 &fz,
                                            f64 &tdu, f64 &vsig_max) {
@@ -234,9 +246,8 @@ __device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace 
         if (rab2 > h_a * h_a * Rker2 && rab2 > h_b * h_b * Rker2) continue;
         f64 rab       = sqrt(rab2);
         const f64 u_b = hs.u[b];
-        f64 rho_b   = rho_h(p.pmass, h_b);
+        f64 rho_b   = PRE ? hs.rho[b] : rho_h(p.pmass, h_b);
         f64 P_b     = hs.P[b];
-        f64 omega_b = hs.omega[b];
         f64 cs_b    = hs.cs[b];
         f64 Fab_a   = dW_3d(rab, h_a);
         f64 Fab_b   = dW_3d(rab, h_b);
@@ -257,9 +268,14 @@ __device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace 
         f64 AV_P_a  = P_a + qa_ab;
         f64 AV_P_b  = P_b + qb_ab;
         f64 sub_fact_a = rho_a_sq * omega_a;
-        f64 sub_fact_b = (rho_b * rho_b) * omega_b;
         f64 ca = AV_P_a * inv_sat_zero(sub_fact_a);
-        f64 cb = AV_P_b * inv_sat_zero(sub_fact_b);
+        f64 cb;
+        if (PRE) {
+            cb = AV_P_b * hs.inv_sub[b];
+        } else {
+            f64 sub_fact_b = (rho_b * rho_b) * hs.omega[b];
+            cb = AV_P_b * inv_sat_zero(sub_fact_b);
+        }
         f64 nax = rx * Fab_a, nay = ry * Fab_a, naz = rz * Fab_a;
         f64 nbx = rx * Fab_b, nby = ry * Fab_b, nbz = rz * Fab_b;
         f64 mb = -p.pmass;
@@ -269,7 +285,7 @@ __device__ __forceinline__ void derivs_row(const RowSpace &rs, const HydroSpace 
         f64 dotvg = vx * nax + vy * nay + vz * naz;
         tdu += AV_P_a * (omega_a_rho_a_inv * rho_a_inv) * p.pmass * dotvg;
         f64 Fa = Fab_a * omega_a_rho_a_inv;
-        f64 Fb = Fab_b / (rho_b * omega_b);
+        f64 Fb = Fab_b / (PRE ? hs.rho_om[b] : rho_b * hs.omega[b]);
         tdu += p.pmass * p.alpha_u * vsig_u * (u_a - u_b) * f64(0.5) * (Fa + Fb);
         if (VSIG) {
             // separate v_sig kernel of the reference: r_hat = dr / r, zero below 1e-9,
@@ -305,6 +321,7 @@ __global__ void __launch_bounds__(128) k_derivs(RowSpace rs, HydroSpace hs, Deri
 // pipeline form: derivatives + v_sig + leapfrog corrector + CFL, outputs to the
 // caller's local arrays.  Neighbour velocities come from the rank-ordered copy
 // taken before the corrector, so correcting the caller's v here is race-free.
+template<bool PRE>
 __global__ void __launch_bounds__(128) k_derivs_step(RowSpace rs, HydroSpace hs, DerivParams p,
                                                      LocalFields lf, Scalars *sc) {
     u32 t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,7 +331,7 @@ __global__ void __launch_bounds__(128) k_derivs_step(RowSpace rs, HydroSpace hs,
         u32 a  = rs.row_rank[t];
         u32 k0 = rs.off[t], k1 = k0 + rs.cnt[t];
         f64 fx, fy, fz, tdu, vm;
-        derivs_row<true>(rs, hs, a, k0, k1, p, fx, fy, fz, tdu, vm);
+        derivs_row<true, PRE>(rs, hs, a, k0, k1, p, fx, fy, fz, tdu, vm);
         u32 i  = rs.row_local[t];
         size_t iv = (size_t) i * lf.vs;
         if (p.ext.x) {
@@ -673,7 +690,8 @@ cudaError_t gather_eos64(Ctx &c, u32 N, u32 n_local, const LocalFields &lf, cons
         c.sort_index.as<u32>(), N, n_local, c.ghost_src.as<u32>(), lf.h, lf.u, lf.vx, lf.vy, lf.vz,
         lf.vs, omega_local, pmass, eos, c.sx.as<f64>(), c.sy.as<f64>(), c.sz.as<f64>(),
         c.sh2.as<f64>(), c.su.as<f64>(), c.svx.as<f64>(), c.svy.as<f64>(), c.svz.as<f64>(),
-        c.som.as<f64>(), c.sP.as<f64>(), c.scs.as<f64>()); GBSPH_COUNTED; }
+        c.som.as<f64>(), c.sP.as<f64>(), c.scs.as<f64>(), c.srho.as<f64>(), c.sinv.as<f64>(),
+        c.srom.as<f64>()); GBSPH_COUNTED; }
     return cudaGetLastError();
 }
 cudaError_t eos_lp07(Ctx &c, u32 n, const f64 *x, const f64 *y, const f64 *z, u32 vs, const f64 *h,
@@ -692,7 +710,11 @@ cudaError_t derivs_step64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, f64 
                           const LocalFields &lf, const ExtAccel &ext) {
     DerivParams p{pmass, alpha_u, alpha_AV, beta_AV, hdt, C_cour, C_force, ext};
     ProfScope ps(c, kProfDerivs, rs.n);
-    { k_derivs_step<<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, lf, c.d_scalars.as<Scalars>()); GBSPH_COUNTED; }
+    if (hs.rho && hs.inv_sub && hs.rho_om) {
+        k_derivs_step<true><<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, lf, c.d_scalars.as<Scalars>()); GBSPH_COUNTED;
+    } else {
+        k_derivs_step<false><<<div_up(rs.n, 128), 128, 0, c.stream>>>(rs, hs, p, lf, c.d_scalars.as<Scalars>()); GBSPH_COUNTED;
+    }
     return cudaGetLastError();
 }
 // leapfrog corrector (integrators.cpp:88-120): v += dt/2 (a_new - a_old), u likewise;

@@ -28,6 +28,10 @@ struct RowSpace {
 struct HydroSpace {
     const f64 *h, *u, *vx, *vy, *vz, *omega, *P, *cs;
     const f64 *alpha;
+    // optional per-particle factors of the FP64 pair loop, computed once by the staging
+    // pass with the pair loop's own expressions (so the same bits): rho_h(m, h),
+    // inv_sat_zero(rho^2 Omega) and rho Omega
+    const f64 *rho, *inv_sub, *rho_om;
 };
 
 // Equation of state of the step: adiabatic (P = (gamma - 1) rho u) or locally
