@@ -406,10 +406,8 @@ __global__ void __launch_bounds__(128) k_owner(TreeView t, const NodeBoxF *__res
 // decides.  The cache is therefore identical to the FP64 one.
 enum CacheMode { kCount = 0, kFill = 1, kOnePass = 2 };
 
-// eight 256-thread blocks per SM (32 registers: the whole SM's warps in flight for the
-// gathers; a few bytes spill): 2-3 % faster than six blocks at 40 registers
 template<int MODE, bool F32>
-__global__ void __launch_bounds__(256, 8) k_part_cache(
+__global__ void __launch_bounds__(256) k_part_cache(
     const u32 *__restrict__ row_rank, u32 n_rows, const u32 *__restrict__ owner,
     const u32 *__restrict__ leaf_cnt, const u32 *__restrict__ leaf_off,
     const uint2 *__restrict__ leaf_ent, const float4 *__restrict__ P,
