@@ -177,3 +177,51 @@ def test_sedov_refresh_every_fourth_step(n_cells):
     logs = [mg.evolve_once() for _ in range(9)]
     assert [g["est_refreshed"] for g in logs] == [1, 0, 0, 0, 1, 0, 0, 0, 1]
     assert _refresh_replay(logs, TOL) == 6
+
+
+@pytest.mark.parametrize("av", ["cd10", "mm97"])
+def test_sound_wave_guarded_varying_viscosity(av):
+    """The error control with the varying viscosity switches: on the sound wave the FP32
+    tier's estimate exceeds the tolerance, the steps run compensated with per-particle
+    alpha and the stored sound speed, and a, du/dt and the updated alpha stay within 1e-5
+    of the FP64 step (normalised by each field's largest magnitude)."""
+    import shamrock_gb300 as sg
+
+    s = _sound_wave()
+    n = len(s["h"])
+    par = dict(alpha_min=0.02, alpha_max=1.0, sigma_decay=0.1, alpha_u=1.0, beta_AV=2.0)
+
+    def model(precision):
+        ctx = sg.Context()
+        m = sg.get_Model_SPH(context=ctx, vector_type="f64_3", sph_kernel="M4")
+        cfg = m.gen_default_config()
+        if av == "cd10":
+            cfg.set_artif_viscosity_VaryingCD10(**par)
+        else:
+            cfg.set_artif_viscosity_VaryingMM97(**par)
+        cfg.set_boundary_periodic()
+        cfg.set_eos_adiabatic(s["gamma"])
+        cfg.set_particle_mass(s["pmass"])
+        cfg.set_precision(precision)
+        m.set_solver_config(cfg)
+        m.resize_simulation_box(s["box_min"], s["box_max"])
+        m.set_particles(s["pos"], s["vel"], s["h"], s["u"], alpha=np.full(n, 0.1))
+        m._to_host()
+        m._host["soundspeed"][:] = 1.0
+        m.set_cfl_cour(0.3)
+        m.set_cfl_force(0.3)
+        return m
+
+    m64, mg = model("fp64"), model("mixed")
+    for step in range(2):
+        m64.evolve_once()
+        lg = mg.evolve_once()
+        assert lg["tier"] == 2, lg
+        ref, d = m64.collect_data(), mg.collect_data()
+        for key in ("axyz", "duint", "alpha_AV"):
+            x, y = d[key], ref[key]
+            if x.ndim > 1:
+                err = np.linalg.norm(x - y, axis=1).max() / np.linalg.norm(y, axis=1).max()
+            else:
+                err = np.abs(x - y).max() / max(np.abs(y).max(), 1e-300)
+            assert err <= TOL, (step, key, err)
