@@ -56,3 +56,32 @@ def test_header_compiles_as_c(tmp_path):
     r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
                         "-c", str(src), "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes mirror of a header struct has the C struct's size and the C offset of
+    each of its fields (the drop-in boundary passes these structs by pointer)."""
+    import ctypes as C
+
+    from shamrock_gb300 import _lib
+
+    pairs = [("gbsph_vec3", _lib.Vec3), ("gbsph_particles", _lib.Particles),
+             ("gbsph_config", _lib.Config), ("gbsph_time_state", _lib.TimeState),
+             ("gbsph_step_log", _lib.StepLog), ("gbsph_cotangents", _lib.Cotangents)]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gbsph.h"', "int main(void){"]
+    expect = []
+    for cname, py in pairs:
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        expect.append(C.sizeof(py))
+        for fname, _ in py._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {fname}));')
+            expect.append(getattr(py, fname).offset)
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert got == expect
