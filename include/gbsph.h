@@ -399,6 +399,21 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
                        double t, double dt, uint32_t corrector_iters, gbsph_cotangents *cot,
                        double *g_alpha_av, void *stream);
 
+/* gbsph_adjoint_step in two halves, for a rollout that keeps several steps recorded at
+ * once (one context per step): gbsph_adjoint_record recomputes the step from `start`
+ * with its tape, keeps what the reverse pass needs in the context (tree, neighbour cache,
+ * h, Omega, the tape, and the recomputed state after the step, which stays valid until
+ * the context records again) and, when `after` is given, points it at that state; the
+ * state after one step is the start state of the next, so a segment of steps is
+ * recomputed once.  gbsph_adjoint_reverse then reverses the recorded step (same `start`,
+ * cfg->precision and dt; GBSPH_ERR_STATE without a recording).  Record followed by
+ * reverse on one context is gbsph_adjoint_step. */
+int gbsph_adjoint_record(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                         double t, double dt, uint32_t corrector_iters, gbsph_particles *after,
+                         void *stream);
+int gbsph_adjoint_reverse(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                          double dt, gbsph_cotangents *cot, double *g_alpha_av, void *stream);
+
 /* ------------------------------------------------------------------ instrumentation
  * Per-stage device time measured with CUDA events on the launching stream (the role
  * of the reference's per-step timers, SolverStorage.hpp:111-118).  Enabling resets the

@@ -117,6 +117,10 @@ SIGNATURES = {
     "gbsph_cfl": (C.c_int, [_vp, _vp, _vp, Vec3, _u32, _f64, _f64, _vp, _P(_f64), _vp]),
     "gbsph_adjoint_step": (C.c_int, [_vp, _P(Particles), _P(Config), _f64, _f64, _u32,
                                      _P(Cotangents), _P(_f64), _vp]),
+    "gbsph_adjoint_record": (C.c_int, [_vp, _P(Particles), _P(Config), _f64, _f64, _u32,
+                                       _P(Particles), _vp]),
+    "gbsph_adjoint_reverse": (C.c_int, [_vp, _P(Particles), _P(Config), _f64, _P(Cotangents),
+                                        _P(_f64), _vp]),
     "gbsph_profile_kinds": (_u32, []),
     "gbsph_kernel_launches": (_u64, []),
     "gbsph_set_cache_budget": (C.c_int, [_vp, _u64]),

@@ -20,8 +20,12 @@ forward pass records the dt sequence; pass it back as ``dts`` to replay the same
 (e.g. for finite-difference checks), since the CFL dt itself is not differentiated.
 
 Memory: the state (x, v, a, h, u, du) is kept every ``checkpoint_every`` steps; the
-backward pass recomputes each segment from its checkpoint and reverses it step by step
-(``gbsph_adjoint_step`` recomputes the step once more on the device with its tape).
+backward pass recomputes each segment from its checkpoint once, each step with its tape
+on a library context of its own (``gbsph_adjoint_record``: the context keeps the step's
+tree, neighbour cache, h, Omega and tape, and the state after the step, which starts the
+next one), then reverses the segment's steps in turn on those contexts
+(``gbsph_adjoint_reverse``).  The model keeps ``checkpoint_every`` such contexts for
+its later backward passes.
 """
 
 import ctypes as C
@@ -104,6 +108,18 @@ def adjoint_step(model, start, t, dt, corrector_iters, cot, tier=None):
     return g_alpha.value
 
 
+def _record_contexts(model, k):
+    """k library contexts on the model's device for the steps of a segment (kept on the
+    model, grown as needed)."""
+    pool = getattr(model, "_adj_pool", None)
+    if pool is None:
+        pool = model._adj_pool = []
+    dev = model._lib().device
+    while len(pool) < k:
+        pool.append(L.Context(dev))
+    return pool
+
+
 def _step(model, t, dt, tier=None):
     model.time = float(t)
     model.dt = float(dt)
@@ -141,25 +157,39 @@ class _Rollout:
         import torch
 
         m = self.model
-        saved = _snapshot(m)
-        saved_time = (m.time, m.dt, m.cfl_mult)
+        pool = _record_contexts(m, self.k)
         g_alpha = 0.0
         starts = sorted(self.checkpoints)
+        torch.cuda.synchronize()
         for s0 in reversed(starts):
             s1 = min(s0 + self.k, self.n_steps)
-            # states at the start of each step of the segment
-            _restore(m, self.checkpoints[s0])
-            seg = []
+            # the segment recomputed once: step j recorded on pool[j - s0], from the state
+            # the previous step's context holds after its step
+            start = _particles_of(self.checkpoints[s0])
+            rec = []
             for j in range(s0, s1):
-                seg.append(_snapshot(m))
-                t, dt, _, tier = self.records[j]
-                if j + 1 < s1:
-                    _step(m, t, dt, tier)
+                t, dt, kk, tier = self.records[j]
+                cfg = m._config_struct(tier)
+                after = L.Particles()
+                ctx = pool[j - s0]
+                ctx.check(ctx.lib.gbsph_adjoint_record(ctx.handle, C.byref(start), C.byref(cfg),
+                                                       float(t), float(dt), int(kk),
+                                                       C.byref(after), None))
+                rec.append((start, cfg))
+                start = after
             for j in reversed(range(s0, s1)):
                 t, dt, kk, tier = self.records[j]
-                g_alpha += adjoint_step(m, seg[j - s0], t, dt, kk, cot, tier)
-        _restore(m, saved)
-        m.time, m.dt, m.cfl_mult = saved_time
+                start, cfg = rec[j - s0]
+                ctx = pool[j - s0]
+                cs = _cot_struct(cot)
+                g = C.c_double(0.0)
+                ctx.check(ctx.lib.gbsph_adjoint_reverse(ctx.handle, C.byref(start), C.byref(cfg),
+                                                        float(dt), C.byref(cs), C.byref(g), None))
+                if "g_av" in cot:
+                    cot["g_av"][0] += cs.g_alpha_min
+                    cot["g_av"][1] += cs.g_alpha_max
+                    cot["g_av"][2] += cs.g_sigma_decay
+                g_alpha += g.value
         torch.cuda.synchronize()
         return g_alpha
 

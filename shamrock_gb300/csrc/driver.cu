@@ -15,6 +15,14 @@
 
 struct gbsph_ctx {
     gbsph::Ctx c;
+    // the step recorded by gbsph_adjoint_record for gbsph_adjoint_reverse: its tape, the
+    // recomputed state after the step (in c.adj_state), and what the reverse must match
+    gbsph::StepTape adj_tape;
+    gbsph_particles adj_after{};
+    bool adj_ready   = false;
+    bool adj_var     = false;
+    uint32_t adj_n   = 0, adj_prec = 0;
+    double adj_dt    = 0;
 };
 
 namespace gbsph {
@@ -1067,17 +1075,16 @@ int gbsph_evolve_once(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_conf
     return evolve_impl(ctx, p, cfg, ts, log, nullptr);
 }
 
-int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
-                       double t, double dt, uint32_t corrector_iters, gbsph_cotangents *cot,
-                       double *g_alpha_av, void *stream) {
+int gbsph_adjoint_record(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                         double t, double dt, uint32_t corrector_iters, gbsph_particles *after,
+                         void *stream) {
     ENTER(ctx, stream);
     Ctx &c = ctx->c;
-    REQUIRE_ARG(start && cfg && cot, "null argument");
-    REQUIRE_ARG(start->n > 0 && cot->n == start->n, "cotangents and state differ in size");
+    ctx->adj_ready = false;
+    REQUIRE_ARG(start && cfg, "null argument");
+    REQUIRE_ARG(start->n > 0, "empty patch");
     REQUIRE_ARG(corrector_iters >= 1 && corrector_iters <= kTapeMaxIters,
                 "corrector_iters must be the forward step's count (1..16)");
-    REQUIRE_ARG(cot->gx.stride == cot->gv.stride && cot->gx.stride == cot->ga.stride,
-                "gx, gv and ga must share one element stride");
     REQUIRE_ARG(dt >= 0, "dt must be the forward step's dt");
     REQUIRE_ARG(cfg->eos_kind == GBSPH_EOS_ADIABATIC || cfg->eos_kind == GBSPH_EOS_LOCALLY_ISOTHERMAL_LP07,
                 "unknown equation of state");
@@ -1086,9 +1093,8 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
                 "the adjoint of the locally isothermal EOS or the point mass needs free "
                 "boundaries (a periodic image's pressure depends on its shifted position)");
     const bool var = cfg->av_kind != GBSPH_AV_CONSTANT;
-    REQUIRE_ARG(!var || (start->alpha_AV && start->soundspeed && cot->galpha && cot->gsoundspeed),
-                "the varying viscosity's adjoint needs alpha_AV and soundspeed in the start state "
-                "and galpha and gsoundspeed in the cotangents");
+    REQUIRE_ARG(!var || (start->alpha_AV && start->soundspeed),
+                "the varying viscosity's adjoint needs alpha_AV and soundspeed in the start state");
     REQUIRE_ARG(cfg->precision != GBSPH_MIXED_GUARDED,
                 "give the adjoint step the tier the forward step ran in (gbsph_step_log.tier)");
     cudaStream_t s = c.stream;
@@ -1118,13 +1124,44 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
         w.soundspeed = W + 13 * n_;
     }
     gbsph_time_state ts{t, dt, 1.0};
-    StepTape tape;
+    StepTape &tape = ctx->adj_tape;
+    tape           = StepTape{};
     tape.forced_iters = corrector_iters;
     tape.snap         = &c.adj_snap;
     tape.snap_av      = &c.adj_snap_av;
     tape.snap_vg      = &c.adj_snap_vg;
     int st = evolve_impl(ctx, &w, cfg, &ts, nullptr, &tape);
     if (st != GBSPH_OK) return st;
+    ctx->adj_after = w;
+    ctx->adj_ready = true;
+    ctx->adj_var   = var;
+    ctx->adj_n     = n;
+    ctx->adj_prec  = cfg->precision;
+    ctx->adj_dt    = dt;
+    if (after) *after = w;
+    return GBSPH_OK;
+}
+
+int gbsph_adjoint_reverse(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                          double dt, gbsph_cotangents *cot, double *g_alpha_av, void *stream) {
+    ENTER(ctx, stream);
+    Ctx &c = ctx->c;
+    REQUIRE_ARG(start && cfg && cot, "null argument");
+    if (!ctx->adj_ready)
+        return fail(ctx, GBSPH_ERR_STATE, "gbsph_adjoint_reverse needs the step recorded by "
+                                          "gbsph_adjoint_record on this context");
+    REQUIRE_ARG(start->n == ctx->adj_n && cot->n == start->n, "cotangents and state differ in size");
+    REQUIRE_ARG(cfg->precision == ctx->adj_prec && dt == ctx->adj_dt,
+                "the reverse must use the recorded step's precision and dt");
+    REQUIRE_ARG(cot->gx.stride == cot->gv.stride && cot->gx.stride == cot->ga.stride,
+                "gx, gv and ga must share one element stride");
+    const bool var = ctx->adj_var;
+    REQUIRE_ARG(!var || (start->alpha_AV && start->soundspeed && cot->galpha && cot->gsoundspeed),
+                "the varying viscosity's adjoint needs alpha_AV and soundspeed in the start state "
+                "and galpha and gsoundspeed in the cotangents");
+    cudaStream_t s = c.stream;
+    const u32 n    = start->n;
+    const gbsph_particles &w = ctx->adj_after;
     RowSpace rs{n,                  c.row_rank.as<u32>(), c.row_local.as<u32>(),
                 c.csr_cnt.as<u32>(), c.csr_off.as<u32>(), c.csr_ent.as<u32>(),
                 c.sx.as<f64>(),      c.sy.as<f64>(),      c.sz.as<f64>()};
@@ -1152,9 +1189,10 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
     CU(cudaMemsetAsync(&dsc->g_alpha, 0, sizeof(f64), s));
     CU(cudaMemsetAsync(dsc->g_av, 0, 3 * sizeof(f64), s));
     // FP32 reverse pass after either mixed tier's recompute, FP64 after the FP64 one
-    CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), tape, ap, cs, &dsc->g_alpha,
-                        dsc->g_av, cfg->precision != GBSPH_FP64));
+    CU(adjoint_backward(c, rs, n, w.hpart, c.omega_local.as<f64>(), ctx->adj_tape, ap, cs,
+                        &dsc->g_alpha, dsc->g_av, cfg->precision != GBSPH_FP64));
     CU(sync_scalars(c));
+    ctx->adj_ready = false;
     if (g_alpha_av) *g_alpha_av += c.h_scalars->g_alpha;
     if (var) {
         cot->g_alpha_min += c.h_scalars->g_av[0];
@@ -1162,6 +1200,16 @@ int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph
         cot->g_sigma_decay += c.h_scalars->g_av[2];
     }
     return GBSPH_OK;
+}
+
+int gbsph_adjoint_step(gbsph_ctx *ctx, const gbsph_particles *start, const gbsph_config *cfg,
+                       double t, double dt, uint32_t corrector_iters, gbsph_cotangents *cot,
+                       double *g_alpha_av, void *stream) {
+    if (ctx && cot && start && cot->n != start->n)
+        return fail(ctx, GBSPH_ERR_ARG, "cotangents and state differ in size");
+    int st = gbsph_adjoint_record(ctx, start, cfg, t, dt, corrector_iters, nullptr, stream);
+    if (st != GBSPH_OK) return st;
+    return gbsph_adjoint_reverse(ctx, start, cfg, dt, cot, g_alpha_av, stream);
 }
 
 } // extern "C"
