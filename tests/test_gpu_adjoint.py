@@ -348,3 +348,67 @@ def test_disc_adjoint_kinetic_energy_fd():
         errs.append((e64, e32, kind, idx))
     assert max(e[0] for e in errs) < 1e-4, errs
     assert max(e[1] for e in errs) < 1e-2, errs
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed_fp32"])
+def test_record_reverse_equals_adjoint_step(precision):
+    """gbsph_adjoint_record + gbsph_adjoint_reverse on a context of their own give the
+    cotangents of gbsph_adjoint_step bit for bit (and dL/d alpha_AV, a sum the blocks add
+    in arrival order, to round-off); a reverse without a recording is refused
+    (GBSPH_ERR_STATE); the state after a recorded step equals the forward step's."""
+    import ctypes as C
+
+    import torch
+
+    from shamrock_gb300 import _lib as L
+    from shamrock_gb300 import adjoint
+    from shamrock_gb300.adjoint import _cot_struct, _particles_of, _snapshot
+
+    m = make_model(precision=precision)
+    start = _snapshot(m)
+    t, dt = m.time, m.dt
+    log = m.evolve_once()
+    after_fwd = _snapshot(m)
+    N = m.get_total_part_count()
+    dev = start["vxyz"].device
+    rng = np.random.default_rng(11)
+
+    def cot0():
+        c = adjoint._zero_cot(N, dev)
+        c["gv"].copy_(torch.as_tensor(rng.standard_normal((3, N)), device=dev))
+        c["gu"].copy_(torch.as_tensor(rng.standard_normal(N), device=dev))
+        return c
+
+    ref = cot0()
+    cot = {k: v.clone() for k, v in ref.items()}
+    g_ref = adjoint.adjoint_step(m, start, t, dt, log["corrector_iters"], ref, log["tier"])
+
+    ctx = L.Context(0)
+    p = _particles_of(start)
+    cfg = m._config_struct(log["tier"])
+    cs = _cot_struct(cot)
+    g = C.c_double(0.0)
+    rc = ctx.lib.gbsph_adjoint_reverse(ctx.handle, C.byref(p), C.byref(cfg), float(dt),
+                                       C.byref(cs), C.byref(g), None)
+    assert rc == L.GBSPH_ERR_STATE
+    after = L.Particles()
+    ctx.check(ctx.lib.gbsph_adjoint_record(ctx.handle, C.byref(p), C.byref(cfg), float(t),
+                                           float(dt), int(log["corrector_iters"]), C.byref(after),
+                                           None))
+    torch.cuda.synchronize()
+    # the recomputed state after the step is the forward step's, bit for bit
+    class _View:  # a device array the library owns, seen through the CUDA array interface
+        def __init__(self, ptr):
+            self.__cuda_array_interface__ = {"shape": (N,), "typestr": "<f8", "data": (ptr, False),
+                                             "version": 2}
+
+    for k, ptr in (("hpart", after.hpart), ("uint", after.uint), ("duint", after.duint)):
+        got = torch.as_tensor(_View(ptr), device=dev).clone()
+        assert torch.equal(got, after_fwd[k]), k
+    ctx.check(ctx.lib.gbsph_adjoint_reverse(ctx.handle, C.byref(p), C.byref(cfg), float(dt),
+                                            C.byref(cs), C.byref(g), None))
+    torch.cuda.synchronize()
+    for k in ref:
+        assert torch.equal(cot[k], ref[k]), k
+    assert abs(g.value - g_ref) <= 1e-12 * abs(g_ref)
+    ctx.close()
