@@ -19,6 +19,7 @@
 // rho_sum / rho_h and h (d rho / dh) / rho_h, and the CFL step runs in FP32.  FP64 stays
 // on the state (h, x, v, u, a) and on pressure, whose hi/lo pair carries it beyond FP32.
 
+#include "df32.cuh"
 #include "mixed_common.cuh"
 
 namespace gbsph {
@@ -122,39 +123,78 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
     split64(lf.vy[iv], vyh, vyl);
     split64(lf.vz[iv], vzh, vzl);
     h_rank[r] = hh;
-    const f64 hinv    = rcp64(hh);
-    const float hinv_f = __double2float_rn(hinv);
-    const f64 rho      = eos.mh3 * hinv * hinv * hinv;
-    f64 Pr;
-    float cs;
-    if (eos.kind == 1 && E) {
-        // compensated tier: the pressure to FP64 accuracy
-        const f64 Rsq   = sx[r] * sx[r] + sy[r] * sy[r] + sz[r] * sz[r];
-        const f64 cs_sq = eos.cs0sq64 * pow(Rsq * eos.inv_r0sq64, eos.mq64);
-        Pr              = cs_sq * rho;
-        cs              = (float) sqrt(cs_sq);
-    } else if (eos.kind == 1) {
-        float ratio = (xh * xh + yh * yh + zh * zh) * eos.inv_r0sq;
-        float cs_sq = eos.cs0sq * powf(ratio, eos.mq);
-        Pr          = (f64) cs_sq * rho;
-        cs          = sqrtf(cs_sq);
+    float u_hi, u_lo;
+    split64(uu, u_hi, u_lo);
+    float hinv_f, cs, c1, Ph, Pl;
+    f64 hinv = 0, Pr = 0, sub = 0;
+    if (!E) {
+        // The FP32 tier's records need 1/h and c1 to FP32 and P to about 2^-32 (its hi
+        // part and a bfloat16 residual): evaluated in double-float arithmetic on the FP32
+        // pipes from the exact hi/lo splits of h, u, Omega and the constants, which keeps
+        // this pass off GB300's scarce FP64 pipe.
+        float h_hi, h_lo, m_hi, m_lo, o_hi, o_lo;
+        split64(hh, h_hi, h_lo);
+        split64(eos.mh3, m_hi, m_lo);
+        split64(om, o_hi, o_lo);
+        // 1/h: the FP32 reciprocal and one Newton step against the double-float h
+        const float y0 = __frcp_rn(h_hi);
+        const df hy    = df_mul_f(df{h_hi, h_lo}, y0);
+        const df hi_df = fast_two_sum(y0, y0 * ((1.f - hy.hi) - hy.lo));
+        hinv_f         = hi_df.hi;
+        const df rho   = df_mul(df_mul(df_sqr(hi_df), hi_df), df{m_hi, m_lo});
+        df P;
+        if (eos.kind == 1) {
+            const float ratio = (xh * xh + yh * yh + zh * zh) * eos.inv_r0sq;
+            const float cs_sq = eos.cs0sq * powf(ratio, eos.mq);
+            P  = df_mul_f(rho, cs_sq);
+            cs = sqrtf(cs_sq);
+        } else {
+            float g_hi, g_lo;
+            split64(eos.gm1, g_hi, g_lo);
+            P  = df_mul(df_mul(df{g_hi, g_lo}, rho), df{u_hi, u_lo});
+            cs = sqrtf(eos.gg * u_hi);
+        }
+        const df Pn = two_sum(P.hi, P.lo); // hi: the value rounded to FP32
+        Ph = Pn.hi;
+        Pl = Pn.lo;
+        // c1 = inv_sat_zero(rho^2 Omega): the FP32 reciprocal refined once
+        const df sd = df_mul(df_sqr(rho), df{o_hi, o_lo});
+        c1          = 0.f;
+        if (sd.hi != 0.f && isfinite(sd.hi)) {
+            const float s0 = __frcp_rn(sd.hi);
+            const df sy    = df_mul_f(sd, s0);
+            c1             = s0 + s0 * ((1.f - sy.hi) - sy.lo);
+        }
     } else {
-        Pr = eos.gm1 * rho * uu;
-        cs = sqrtf(eos.gg * __double2float_rn(uu));
+        hinv   = rcp64(hh);
+        hinv_f = __double2float_rn(hinv);
+        const f64 rho = eos.mh3 * hinv * hinv * hinv;
+        if (eos.kind == 1) {
+            // compensated tier: the pressure to FP64 accuracy
+            const f64 Rsq   = sx[r] * sx[r] + sy[r] * sy[r] + sz[r] * sz[r];
+            const f64 cs_sq = eos.cs0sq64 * pow(Rsq * eos.inv_r0sq64, eos.mq64);
+            Pr              = cs_sq * rho;
+            cs              = (float) sqrt(cs_sq);
+        } else {
+            Pr = eos.gm1 * rho * uu;
+            cs = sqrtf(eos.gg * u_hi);
+        }
+        sub = rho * rho * om;
+        c1  = (sub != 0 && sub == sub) ? __double2float_rn(rcp64(sub)) : 0.f;
+        split64(Pr, Ph, Pl);
     }
-    const f64 sub  = rho * rho * om;
-    const float c1 = (sub != 0 && sub == sub) ? __double2float_rn(rcp64(sub)) : 0.f;
-    float Ph, Pl;
-    split64(Pr, Ph, Pl);
     size_t p2 = 2 * (size_t) r;
     P[p2]     = make_float4(xh, yh, zh, hinv_f);
     P[p2 + 1] = make_float4(xl, yl, zl, cs);
-    H[p2]     = make_float4(vxh, vyh, vzh, __double2float_rn(uu));
+    H[p2]     = make_float4(vxh, vyh, vzh, u_hi);
     H[p2 + 1] = make_float4(Ph, c1, pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, Pl));
     if (av.V) {
-        av.V[p2]     = make_float4(vxh, vyh, vzh, __double2float_rn(av.ax[iv]));
-        av.V[p2 + 1] = make_float4(__double2float_rn(av.ay[iv]), __double2float_rn(av.az[iv]),
-                                   pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, 0.f));
+        float axh, axl, ayh, ayl, azh, azl;
+        split64(av.ax[iv], axh, axl);
+        split64(av.ay[iv], ayh, ayl);
+        split64(av.az[iv], azh, azl);
+        av.V[p2]     = make_float4(vxh, vyh, vzh, axh);
+        av.V[p2 + 1] = make_float4(ayh, azh, pack_bf16x2(vxl, vyl), pack_bf16x2(vzl, 0.f));
         av.cs_rank[r] = cs;
     }
     if (E) {
@@ -166,7 +206,6 @@ __global__ void k_gather_stage_mixed(const u32 *__restrict__ sort_index, u32 N, 
         const f64 hinv2 = hinv * hinv;
         split64(hinv2 * hinv2, h4h, h4l);
         const float hinv_lo = __double2float_rn(hinv - (f64) hinv_f);
-        const float u_lo    = __double2float_rn(uu - (f64) __double2float_rn(uu));
         E[p2]     = make_float4(Xh, Xl, hinv_lo, Pl);
         E[p2 + 1] = make_float4(u_lo, h4h, h4l, 0.f);
     }
