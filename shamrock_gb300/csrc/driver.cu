@@ -860,10 +860,11 @@ static int evolve_tier(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
             }
             if (cfg->av_kind == GBSPH_AV_VARYING_CD10)
                 CU(cd10_update(c, n, divv, cx, cy, cz, cvs, dtdv, p->soundspeed, lf.h, p->alpha_AV,
-                               dt, cfg->sigma_decay, cfg->alpha_min, cfg->alpha_max, alpha_upd));
+                               dt, cfg->sigma_decay, cfg->alpha_min, cfg->alpha_max, alpha_upd,
+                               mixed));
             else
                 CU(mm97_update(c, n, divv, p->soundspeed, lf.h, p->alpha_AV, dt, cfg->sigma_decay,
-                               cfg->alpha_min, cfg->alpha_max, alpha_upd));
+                               cfg->alpha_min, cfg->alpha_max, alpha_upd, mixed));
             if (mixed) {
                 CU(stage_alpha_mixed(c, N, n, alpha_upd));
             } else {

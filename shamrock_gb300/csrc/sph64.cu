@@ -580,48 +580,57 @@ __global__ void __launch_bounds__(128) k_velgrad64(RowSpace rs, HydroSpace hs,
 
 // Cullen & Dehnen (2010) switch, one implicit-Euler step (UpdateViscosity.cpp:170-215);
 // max / min as comparisons, as in the oracle
+// T = f64: the reference's FP64 switch, bit for bit.  T = float: the same expressions in
+// FP32 for the mixed path (its velocity gradients are FP32 sums already; the switch's
+// divisions would otherwise make this pass FP64-pipe bound on GB300).
+template<class T>
 __global__ void k_cd10(u32 n, const f64 *__restrict__ divv, const f64 *__restrict__ cx,
                        const f64 *__restrict__ cy, const f64 *__restrict__ cz, u32 cvs,
                        const f64 *__restrict__ dtdivv, const f64 *__restrict__ cs,
-                       const f64 *__restrict__ h, const f64 *__restrict__ alpha, f64 dt,
-                       f64 sigma_decay, f64 alpha_min, f64 alpha_max, f64 *__restrict__ alpha_new) {
+                       const f64 *__restrict__ h, const f64 *__restrict__ alpha, f64 dt_,
+                       f64 sigma_decay_, f64 alpha_min_, f64 alpha_max_, f64 *__restrict__ alpha_new) {
     u32 i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const f64 eps  = 2.220446049250313e-16; // DBL_EPSILON
-    const f64 cs_a = cs[i], h_a = h[i], alpha_a = alpha[i];
-    const f64 inv_tau = cs_a * sigma_decay / h_a;
-    const f64 fact_t  = dt * inv_tau;
-    const f64 euler   = 1 / (1 + fact_t);
-    const f64 md = -divv[i];
-    f64 fac      = (md > 0) ? md : f64(0);
-    fac          = fac * fac;
-    const size_t iv  = (size_t) i * cvs;
-    const f64 traceS = (cx[iv] * cx[iv] + cy[iv] * cy[iv]) + cz[iv] * cz[iv];
-    const f64 balsara = (fac + traceS > eps) ? fac / (fac + traceS) : f64(1);
-    const f64 mdt     = -dtdivv[i];
-    const f64 A       = balsara * ((mdt > 0) ? mdt : f64(0));
-    const f64 temp    = cs_a * cs_a;
-    f64 alpha_loc     = (cs_a > 0) ? 10 * h_a * h_a * A / temp : alpha_min;
-    alpha_loc         = (alpha_loc < alpha_max) ? alpha_loc : alpha_max;
-    alpha_loc         = (temp > eps) ? alpha_loc : alpha_min;
-    f64 na = (alpha_a + alpha_loc * fact_t) * euler;
+    const T eps  = (T) 2.220446049250313e-16; // DBL_EPSILON
+    const T dt = (T) dt_, sigma_decay = (T) sigma_decay_, alpha_min = (T) alpha_min_,
+            alpha_max = (T) alpha_max_;
+    const T cs_a = (T) cs[i], h_a = (T) h[i], alpha_a = (T) alpha[i];
+    const T inv_tau = cs_a * sigma_decay / h_a;
+    const T fact_t  = dt * inv_tau;
+    const T euler   = 1 / (1 + fact_t);
+    const T md = -(T) divv[i];
+    T fac      = (md > 0) ? md : T(0);
+    fac        = fac * fac;
+    const size_t iv = (size_t) i * cvs;
+    const T cxi = (T) cx[iv], cyi = (T) cy[iv], czi = (T) cz[iv];
+    const T traceS  = (cxi * cxi + cyi * cyi) + czi * czi;
+    const T balsara = (fac + traceS > eps) ? fac / (fac + traceS) : T(1);
+    const T mdt     = -(T) dtdivv[i];
+    const T A       = balsara * ((mdt > 0) ? mdt : T(0));
+    const T temp    = cs_a * cs_a;
+    T alpha_loc     = (cs_a > 0) ? 10 * h_a * h_a * A / temp : alpha_min;
+    alpha_loc       = (alpha_loc < alpha_max) ? alpha_loc : alpha_max;
+    alpha_loc       = (temp > eps) ? alpha_loc : alpha_min;
+    T na = (alpha_a + alpha_loc * fact_t) * euler;
     if (alpha_loc > alpha_a) na = alpha_loc;
-    alpha_new[i] = na;
+    alpha_new[i] = (f64) na;
 }
 
 // Morris & Monaghan (1997) switch (UpdateViscosity.cpp:53-118), comparisons as in the oracle
+template<class T>
 __global__ void k_mm97(u32 n, const f64 *__restrict__ divv, const f64 *__restrict__ cs,
-                       const f64 *__restrict__ h, const f64 *__restrict__ alpha, f64 dt,
-                       f64 sigma_decay, f64 alpha_min, f64 alpha_max, f64 *__restrict__ alpha_new) {
+                       const f64 *__restrict__ h, const f64 *__restrict__ alpha, f64 dt_,
+                       f64 sigma_decay_, f64 alpha_min_, f64 alpha_max_, f64 *__restrict__ alpha_new) {
     u32 i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const f64 inv_tau = cs[i] * sigma_decay / h[i];
-    const f64 fact_t  = dt * inv_tau;
-    const f64 euler   = 1 / (1 + fact_t);
-    const f64 md      = -divv[i];
-    const f64 source  = (md > 0) ? md : f64(0);
-    const f64 na      = (alpha[i] + source * dt + fact_t * alpha_min) * euler;
-    alpha_new[i]      = (na < alpha_max) ? na : alpha_max;
+    const T dt = (T) dt_, alpha_min = (T) alpha_min_, alpha_max = (T) alpha_max_;
+    const T inv_tau = (T) cs[i] * (T) sigma_decay_ / (T) h[i];
+    const T fact_t  = dt * inv_tau;
+    const T euler   = 1 / (1 + fact_t);
+    const T md      = -(T) divv[i];
+    const T source  = (md > 0) ? md : T(0);
+    const T na      = ((T) alpha[i] + source * dt + fact_t * alpha_min) * euler;
+    alpha_new[i]    = (f64) ((na < alpha_max) ? na : alpha_max);
 }
 
 __global__ void k_gather_merged(const u32 *__restrict__ sort_index, u32 N, u32 n_local,
@@ -799,17 +808,28 @@ cudaError_t velgrad64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, const f6
 cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64 *cy,
                         const f64 *cz, u32 cvs, const f64 *dtdivv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
-                        f64 *alpha_new) {
-    { k_cd10<<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cx, cy, cz, cvs, dtdivv, cs, h, alpha,
-                                                  dt, sigma_decay, alpha_min, alpha_max,
-                                                  alpha_new); GBSPH_COUNTED; }
+                        f64 *alpha_new, bool fp32) {
+    if (fp32) {
+        k_cd10<float><<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cx, cy, cz, cvs, dtdivv, cs, h,
+                                                           alpha, dt, sigma_decay, alpha_min,
+                                                           alpha_max, alpha_new); GBSPH_COUNTED;
+    } else {
+        k_cd10<f64><<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cx, cy, cz, cvs, dtdivv, cs, h,
+                                                         alpha, dt, sigma_decay, alpha_min,
+                                                         alpha_max, alpha_new); GBSPH_COUNTED;
+    }
     return cudaGetLastError();
 }
 cudaError_t mm97_update(Ctx &c, u32 n, const f64 *divv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
-                        f64 *alpha_new) {
-    { k_mm97<<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cs, h, alpha, dt, sigma_decay, alpha_min,
-                                                  alpha_max, alpha_new); GBSPH_COUNTED; }
+                        f64 *alpha_new, bool fp32) {
+    if (fp32) {
+        k_mm97<float><<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cs, h, alpha, dt, sigma_decay,
+                                                           alpha_min, alpha_max, alpha_new); GBSPH_COUNTED;
+    } else {
+        k_mm97<f64><<<div_up(n, 256), 256, 0, c.stream>>>(n, divv, cs, h, alpha, dt, sigma_decay,
+                                                         alpha_min, alpha_max, alpha_new); GBSPH_COUNTED;
+    }
     return cudaGetLastError();
 }
 cudaError_t conservation64(Ctx &c, const LocalFields &lf, u32 n, f64 pmass, f64 *out_dev,

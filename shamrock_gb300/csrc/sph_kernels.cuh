@@ -95,7 +95,7 @@ cudaError_t velgrad64(Ctx &c, const RowSpace &rs, const HydroSpace &hs, const f6
 cudaError_t cd10_update(Ctx &c, u32 n, const f64 *divv, const f64 *cx, const f64 *cy,
                         const f64 *cz, u32 cvs, const f64 *dtdivv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
-                        f64 *alpha_new);
+                        f64 *alpha_new, bool fp32 = false);
 // conservation totals {sum m v (3), sum m a (3), sum m (u + v.v/2), sum m (v.a + du)} of
 // n local particles into out_dev[8] (scratch: 8 x 1024 doubles), deterministic order
 cudaError_t conservation64(Ctx &c, const LocalFields &lf, u32 n, f64 pmass, f64 *out_dev,
@@ -103,7 +103,7 @@ cudaError_t conservation64(Ctx &c, const LocalFields &lf, u32 n, f64 pmass, f64 
 // the Morris & Monaghan (1997) switch update (UpdateViscosity.cpp:53-118)
 cudaError_t mm97_update(Ctx &c, u32 n, const f64 *divv, const f64 *cs, const f64 *h,
                         const f64 *alpha, f64 dt, f64 sigma_decay, f64 alpha_min, f64 alpha_max,
-                        f64 *alpha_new);
+                        f64 *alpha_new, bool fp32 = false);
 // dst[r] = src[(merged id of rank r) -> local source] * stride, r < N (ghosts copy their source)
 cudaError_t gather_merged64(Ctx &c, u32 N, u32 n_local, const f64 *src, u32 stride, f64 *dst);
 // dst[row_local[t]] = src[row_rank[t]] for the n pipeline rows
