@@ -4,6 +4,7 @@
 #include "../../include/gbsph.h"
 #include "gbsph_ctx.cuh"
 #include "adjoint.cuh"
+#include "guard_rule.h"
 #include "sph_kernels.cuh"
 #include "sph_mixed.cuh"
 
@@ -1049,12 +1050,8 @@ static int evolve_impl(gbsph_ctx *ctx, const gbsph_particles *p, const gbsph_con
     if (refresh) {
         c.guard_est_a  = lg.err_est_a;
         c.guard_est_du = lg.err_est_du;
-        bool skip = tier == GBSPH_MIXED && est <= tol / 8;
-        if (tier == GBSPH_MIXED && !skip && c.guard_prev_est >= 0 && est <= 0.8 * tol) {
-            const f64 rate = std::max(0.0, est - c.guard_prev_est) / f64(c.guard_since);
-            skip = est + 2 * 4 * rate <= 0.8 * tol;
-        }
-        c.guard_skip     = skip ? 3 : 0;
+        c.guard_skip     = guard_refresh_skip(est, c.guard_prev_est, c.guard_since, tol,
+                                              tier == GBSPH_MIXED);
         c.guard_prev_est = tier == GBSPH_MIXED ? est : -1;
         c.guard_since    = 0;
     } else {
