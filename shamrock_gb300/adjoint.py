@@ -25,7 +25,9 @@ on a library context of its own (``gbsph_adjoint_record``: the context keeps the
 tree, neighbour cache, h, Omega and tape, and the state after the step, which starts the
 next one), then reverses the segment's steps in turn on those contexts
 (``gbsph_adjoint_reverse``).  The model keeps ``checkpoint_every`` such contexts for
-its later backward passes.
+its later backward passes.  Past ``MAX_POOLED_PARTICLES`` particles times
+``checkpoint_every`` the backward pass uses the model's own context alone: each segment's
+start states rebuilt with plain steps, then each step recorded and reversed in turn.
 """
 
 import ctypes as C
@@ -108,6 +110,12 @@ def adjoint_step(model, start, t, dt, corrector_iters, cot, tier=None):
     return g_alpha.value
 
 
+# Above this many particles times steps per segment the backward pass records and
+# reverses on one context (a context holds the tree, cache slots and staging of one step:
+# about 5 GB at 4M particles on the homogeneous set-up), else on one context per step.
+MAX_POOLED_PARTICLES = 1 << 25
+
+
 def _record_contexts(model, k):
     """k library contexts on the model's device for the steps of a segment (kept on the
     model, grown as needed)."""
@@ -154,6 +162,39 @@ class _Rollout:
     def backward(self, cot):
         """cot: cotangents of the final state (dict gx, gv, ga, gu, gdu); updated in place
         to the cotangents of the initial state.  Returns dL/d alpha_AV."""
+        n = int(cot["gu"].shape[0])
+        if self.k > 1 and n * self.k > MAX_POOLED_PARTICLES:
+            return self._backward_one_context(cot)
+        return self._backward_pooled(cot)
+
+    def _backward_one_context(self, cot):
+        """The schedule for segments too large to keep a context per step: the segment's
+        start states rebuilt from its checkpoint with plain steps, then each step recorded
+        and reversed on the model's own context (gbsph_adjoint_step)."""
+        import torch
+
+        m = self.model
+        saved = _snapshot(m)
+        saved_time = (m.time, m.dt, m.cfl_mult)
+        g_alpha = 0.0
+        for s0 in reversed(sorted(self.checkpoints)):
+            s1 = min(s0 + self.k, self.n_steps)
+            _restore(m, self.checkpoints[s0])
+            seg = []
+            for j in range(s0, s1):
+                seg.append(_snapshot(m))
+                t, dt, _, tier = self.records[j]
+                if j + 1 < s1:
+                    _step(m, t, dt, tier)
+            for j in reversed(range(s0, s1)):
+                t, dt, kk, tier = self.records[j]
+                g_alpha += adjoint_step(m, seg[j - s0], t, dt, kk, cot, tier)
+        _restore(m, saved)
+        m.time, m.dt, m.cfl_mult = saved_time
+        torch.cuda.synchronize()
+        return g_alpha
+
+    def _backward_pooled(self, cot):
         import torch
 
         m = self.model

@@ -110,3 +110,20 @@ def test_segments_recorded_once_and_reversed(monkeypatch, n_steps, k):
             assert prec == r.records[j][3] and dt == r.records[j][1]
             i += 1
     assert i == len(log)
+
+
+def test_large_segments_use_one_context(monkeypatch):
+    """Past MAX_POOLED_PARTICLES particles times steps per segment the backward pass keeps
+    to the model's own context."""
+    called = []
+    monkeypatch.setattr(adjoint._Rollout, "_backward_one_context", lambda self, cot: called.append("one") or 0.0)
+    monkeypatch.setattr(adjoint._Rollout, "_backward_pooled", lambda self, cot: called.append("pool") or 0.0)
+    r = adjoint._Rollout(_FakeModel(), 10, 5)
+    cot = adjoint._zero_cot(8, "cpu")
+    monkeypatch.setattr(adjoint, "MAX_POOLED_PARTICLES", 40)
+    r.backward(cot)
+    monkeypatch.setattr(adjoint, "MAX_POOLED_PARTICLES", 39)
+    r.backward(cot)
+    r1 = adjoint._Rollout(_FakeModel(), 10, 1)  # one step per segment: one context anyway
+    r1.backward(cot)
+    assert called == ["pool", "one", "pool"]
